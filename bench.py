@@ -1,0 +1,369 @@
+#!/usr/bin/env python
+"""Benchmark of the particle-DEM step (one ParticleSystem::update per step).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload: the plain DEM at scale -- 4,194,304 spheres with lognormal radii
+(median 1/512, sigma 0.25, clipped at 2/512), 256^3 grid sized to the max
+diameter, seeded random packing at 30% volume fraction, contact parameters
+spring 0.5, damping 0.02, shear 0.1, attraction 0, boundary damping -0.5,
+gravity -3e-4, dt 0.5.  Synthetic, seeded (no dataset exists for this path).
+
+Metric: particle-steps/s (higher is better).  `value` is device-resident: K
+fused updates (fcdemUpdate) bracketed by CUDA events on the launching stream.
+`e2e` is the same metric through the reference-named C-ABI with host buffers:
+per step copyArrayToDevice of pos and vel from pinned memory, one update,
+copyArrayFromDevice of pos and vel.  The working set (~560 MB) exceeds the
+129 MB L2, so no flush is needed between steps.
+
+--impl reference times the reference's CPU implementation of the step (the C
+restatement of cuda_addon/particles_kernel.cu in oracle/, using all host
+threads for the collide stage) on a bounded sample: each step is one full
+update of the same scene.  Multi-GPU (torchrun): independent replicas, one per
+rank, no collective on the data path; value sums the ranks' particle-steps.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("particle-steps/s on 1 GB300: batched+neural-SDF vs plain at "
+          "≤1e-5 rel force err")
+UNIT = "particle-steps/s"
+WORKLOAD = "plain DEM at scale: 4,194,304 lognormal spheres, 256^3 grid, 30% packing"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=4194304, help="particles (default: the full workload)")
+    ap.add_argument("--cpu-steps", type=int, default=20, help="CPU-baseline sample steps")
+    ap.add_argument("--cpu-budget-s", type=float, default=150.0,
+                    help="time cap of the reference arm's timed steps")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def load_scene(n: int) -> dict:
+    """config1 scene, cached on local disk (packing 4M spheres takes ~15 s)."""
+    from fullc0ntact_gb300 import scenes
+    from fullc0ntact_gb300.params import SimParams
+    path = os.path.join(tempfile.gettempdir(), f"fcdem_scene_packed_{n}_v1.npz")
+    if os.path.exists(path):
+        try:
+            with np.load(path) as z:
+                return dict(name=str(z["name"]), pos=z["pos"], vel=z["vel"],
+                            params=SimParams.from_buffer_copy(z["params"].tobytes()),
+                            radius_from_w=True, dt=float(z["dt"]))
+        except Exception:
+            pass
+    sc = scenes.config1(n)
+    tmp = path + f".{os.getpid()}.tmp.npz"
+    np.savez(tmp, name=sc["name"], pos=sc["pos"], vel=sc["vel"],
+             params=np.frombuffer(bytes(sc["params"]), np.uint8), dt=sc["dt"])
+    os.replace(tmp, path)
+    return sc
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict | None:
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, flag in zip(names, parts[3:7]):
+                if flag.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak_gbs():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic(kernel: str, n: int):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary
+    (profiles/<kernel>.json: bytes measured on n_measured particles, scaled
+    by the particles processed), or None."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["dram_bytes_per_launch"]) * n / float(d["n"])
+    except Exception:
+        return None
+
+
+def cpu_baseline(sc: dict, steps: int) -> dict:
+    """The oracle (C restatement of the reference step) on this host's cores:
+    `steps` full updates of the same scene."""
+    from oracle import oracle as O
+    P = O.SimParams.from_buffer_copy(bytes(sc["params"]))
+    pos, vel = sc["pos"].copy(), sc["vel"].copy()
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    O.update(P, pos, vel, sc["dt"], steps=steps, radius_from_w=sc["radius_from_w"],
+             nthreads=threads)
+    dt = time.perf_counter() - t0
+    n = pos.shape[0]
+    return {"value": n * steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{steps} full updates of the {n}-sphere scene "
+                      f"(collide on {threads} threads, other stages on 1)",
+            "seconds": dt}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    sc = load_scene(args.n)
+    n = sc["pos"].shape[0]
+    from oracle import oracle as O
+    P = O.SimParams.from_buffer_copy(bytes(sc["params"]))
+    pos, vel = sc["pos"].copy(), sc["vel"].copy()
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    O.update(P, pos, vel, sc["dt"], steps=max(args.warmup, 1), radius_from_w=True,
+             nthreads=threads)
+    per_step = (time.perf_counter() - t0) / max(args.warmup, 1)
+    # bounded sample: all K steps unless they would exceed the time cap
+    steps = max(1, min(args.steps, int(args.cpu_budget_s / max(per_step, 1e-9))))
+    t0 = time.perf_counter()
+    O.update(P, pos, vel, sc["dt"], steps=steps, radius_from_w=True, nthreads=threads)
+    el = time.perf_counter() - t0
+    value = n * steps / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded packing)",
+        "config": {"workload": WORKLOAD, "n": n, "grid": 256, "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{steps} of {args.steps} steps timed, each a full update "
+                                   f"of the {n}-sphere scene (collide on {threads} threads, "
+                                   f"other stages on 1)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.cuda.current_device()
+
+    from fullc0ntact_gb300 import dem
+    lib = dem.lib
+    lib.fcdemGetLaunchCount.restype = C.c_ulonglong
+    lib.fcdemSetProfiling.argtypes = [C.c_int]
+    lib.fcdemGetStageTimes.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_uint), C.c_int]
+
+    sc = load_scene(args.n)
+    n = sc["pos"].shape[0]
+    ds = dem.DeviceScene(sc, f"cuda:{dev}")
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    clocks = ClockSampler(dev)
+    clocks.start()
+    for _ in range(max(args.warmup, 0)):
+        ds.update(1)
+    dem.check("warm-up")
+
+    # --- device-resident timing: K fused updates -------------------------
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    l0 = lib.fcdemGetLaunchCount()
+    start.record()
+    ds.update(args.steps)
+    end.record()
+    barrier()
+    launches = int(lib.fcdemGetLaunchCount() - l0)
+    el_ms = start.elapsed_time(end)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([el_ms], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        el_ms = float(t.item())
+    dem.check("timed updates")
+    value = world * n * args.steps / (el_ms / 1e3)
+
+    # --- stage attribution (same workload, events around each stage) -----
+    lib.fcdemSetProfiling(1)
+    ds.update(args.steps)
+    ms = (C.c_float * 5)()
+    cnt = (C.c_uint * 5)()
+    lib.fcdemGetStageTimes(ms, cnt, 5)
+    lib.fcdemSetProfiling(0)
+    stage_names = ["integrate_hash", "sort", "fill", "reorder", "collide"]
+    stage_ms = {nm: (ms[k] / cnt[k] if cnt[k] else None) for k, nm in enumerate(stage_names)}
+    occupied = int((ds.cell_start != -1).sum().item())
+    ncell = ds.num_cells
+    # algorithmic bytes per launch (each ABI element touched once)
+    algo = {
+        "integrate_hash": 72 * n,
+        "sort": 16 * n,
+        "fill": 4 * ncell,
+        "reorder": 72 * n + 8 * occupied,
+        # fused collide: sorted pos/vel 32, index 4, new vel 16, new pos 16,
+        # next hash 4 per particle; cellStart/cellEnd of occupied cells
+        "collide": 72 * n + 8 * occupied,
+    }
+    dominant = max((k for k in stage_names if stage_ms[k]), key=lambda k: stage_ms[k])
+    peak, peak_kind = measured_peak_gbs()
+    achieved = algo[dominant] / (stage_ms[dominant] / 1e3) / 1e9
+    traffic = profile_traffic(f"fcdem_{dominant}", n)
+
+    # --- end to end through the C-ABI with host buffers --------------------
+    hpos = torch.empty((n, 4), dtype=torch.float32).pin_memory()
+    hvel = torch.empty((n, 4), dtype=torch.float32).pin_memory()
+    hpos.copy_(torch.from_numpy(sc["pos"]))
+    hvel.copy_(torch.from_numpy(sc["vel"]))
+    nbytes = n * 16
+    e2e_steps = max(1, min(args.steps, 50))
+    ds.activate()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        lib.copyArrayToDevice(ds.pos.data_ptr(), hpos.data_ptr(), 0, nbytes)
+        lib.copyArrayToDevice(ds.vel.data_ptr(), hvel.data_ptr(), 0, nbytes)
+        dem.update(ds.pos, ds.vel, ds.sorted_pos, ds.sorted_vel, ds.hash, ds.index,
+                   ds.cell_start, ds.cell_end, ds.dt, n, ds.num_cells, 1)
+        lib.copyArrayFromDevice(hpos.data_ptr(), ds.pos.data_ptr(), None, nbytes)
+        lib.copyArrayFromDevice(hvel.data_ptr(), ds.vel.data_ptr(), None, nbytes)
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_s], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    dem.check("e2e")
+    e2e = world * n * e2e_steps / e2e_s
+    clk = clocks.stop()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline and world == 1:
+        cpu = cpu_baseline(sc, args.cpu_steps)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded packing)",
+            "config": {"workload": WORKLOAD, "n": n, "grid": 256, "cells": ncell,
+                       "occupied_cells": occupied, "step": "fcdemUpdate (fused update)",
+                       "l2": "inputs larger than L2 (no flush)",
+                       "parallelism": f"replicas x{world}"},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
+                    "d2h_bytes_per_step": 2 * nbytes, "steps": e2e_steps,
+                    "path": "copyArrayToDevice x2, fcdemUpdate, copyArrayFromDevice x2"},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved,
+                         "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_source": peak_kind,
+                         "traffic": traffic, "algorithmic_bytes": algo[dominant],
+                         "avg_launch_ms": stage_ms[dominant]},
+            "stage_ms": stage_ms,
+            "clocks": clk,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

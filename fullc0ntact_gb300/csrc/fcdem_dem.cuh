@@ -1,0 +1,88 @@
+// fcdem_dem.cuh -- per-particle device arithmetic of the DEM step.
+//
+// Each function states the reference routine it reproduces.  The arithmetic
+// is written with the same operations in the same order as the reference, so
+// that the compiler forms the same fused multiply-adds and the results agree
+// bit for bit with the reference kernels built by the same nvcc.
+#pragma once
+
+#include "fcdem_internal.cuh"
+
+namespace fcdem {
+
+__device__ __forceinline__ float4 ldg4(const float4 *p) { return __ldg(p); }
+
+// particles_kernel.cu:78-85 (calcGridPos): IEEE division and floor, then the
+// float->int conversion of the assignment.
+__device__ __forceinline__ int3 gridPos(float px, float py, float pz,
+                                        const SimParams &P) {
+  int3 g;
+  g.x = (int)floorf((px - P.worldOrigin[0]) / P.cellSize[0]);
+  g.y = (int)floorf((py - P.worldOrigin[1]) / P.cellSize[1]);
+  g.z = (int)floorf((pz - P.worldOrigin[2]) / P.cellSize[2]);
+  return g;
+}
+
+// particles_kernel.cu:88-94 (calcGridHash): power-of-two wrap, 24-bit
+// multiplies.
+__device__ __forceinline__ unsigned gridHash(int gx, int gy, int gz,
+                                             const SimParams &P) {
+  unsigned x = (unsigned)gx & (P.gridSize[0] - 1u);
+  unsigned y = (unsigned)gy & (P.gridSize[1] - 1u);
+  unsigned z = (unsigned)gz & (P.gridSize[2] - 1u);
+  return __umul24(__umul24(z, P.gridSize[1]), P.gridSize[0]) +
+         __umul24(y, P.gridSize[0]) + x;
+}
+
+// particles_kernel.cu:39-75 (integrate_functor) on one particle; r is the
+// clamp radius (particleRadius, or pos.w in the polydisperse mode).
+__device__ __forceinline__ void integrateOne(float3 &p, float3 &v, float dt,
+                                             float r, const SimParams &P) {
+  v.x = v.x + P.gravity[0] * dt;
+  v.y = v.y + P.gravity[1] * dt;
+  v.z = v.z + P.gravity[2] * dt;
+  v.x = v.x * P.globalDamping;
+  v.y = v.y * P.globalDamping;
+  v.z = v.z * P.globalDamping;
+  p.x = p.x + v.x * dt;
+  p.y = p.y + v.y * dt;
+  p.z = p.z + v.z * dt;
+  const float bd = P.boundaryDamping;
+  if (p.x > 1.0f - r) { p.x = 1.0f - r; v.x = v.x * bd; }
+  if (p.x < -1.0f + r) { p.x = -1.0f + r; v.x = v.x * bd; }
+  if (p.y > 1.0f - r) { p.y = 1.0f - r; v.y = v.y * bd; }
+  if (p.z > 1.0f - r) { p.z = 1.0f - r; v.z = v.z * bd; }
+  if (p.z < -1.0f + r) { p.z = -1.0f + r; v.z = v.z * bd; }
+  if (p.y < -1.0f + r) { p.y = -1.0f + r; v.y = v.y * bd; }
+}
+
+// The force of particles_kernel.cu:185-218 (collideSpheres) once the
+// distance test has passed: rel = pB - pA, dist = |rel|, cd = rA + rB.
+__device__ __forceinline__ float3 contactTerm(float3 rel, float dist, float cd,
+                                              float3 vA, float3 vB,
+                                              float attraction,
+                                              const SimParams &P) {
+  float inv = 1.0f / dist;
+  float3 nrm = make_float3(rel.x * inv, rel.y * inv, rel.z * inv);
+  float3 rv = make_float3(vB.x - vA.x, vB.y - vA.y, vB.z - vA.z);
+  float dn = rv.x * nrm.x + rv.y * nrm.y + rv.z * nrm.z;
+  float3 tv = make_float3(rv.x - nrm.x * dn, rv.y - nrm.y * dn, rv.z - nrm.z * dn);
+  float s = -P.spring * (cd - dist);
+  float3 f = make_float3(nrm.x * s, nrm.y * s, nrm.z * s);
+  f.x = f.x + rv.x * P.damping;
+  f.y = f.y + rv.y * P.damping;
+  f.z = f.z + rv.z * P.damping;
+  f.x = f.x + tv.x * P.shear;
+  f.y = f.y + tv.y * P.shear;
+  f.z = f.z + tv.z * P.shear;
+  f.x = f.x + rel.x * attraction;
+  f.y = f.y + rel.y * attraction;
+  f.z = f.z + rel.z * attraction;
+  return f;
+}
+
+__device__ __forceinline__ float pairDist(float3 rel) {
+  return sqrtf(rel.x * rel.x + rel.y * rel.y + rel.z * rel.z);
+}
+
+}  // namespace fcdem

@@ -1,0 +1,411 @@
+// fcdem_host.cpp -- host side above the C-ABI: the headless ParticleSystem
+// (cuda_addon/particleSystem.cpp) and the scene generators.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "../../include/fcdem.h"
+#include "../../include/fcdem_particle_system.h"
+
+namespace {
+
+// splitmix64: a small, platform-independent generator.
+typedef unsigned long long u64;
+inline u64 nextU64(u64 &s) {
+  u64 z = (s += 0x9e3779b97f4a7c15ull);
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+// Uniform in [0, 1) with 24 random bits (exact in float).
+inline float uniformF(u64 &s) { return (float)(nextU64(s) >> 40) * (1.0f / 16777216.0f); }
+inline double uniformD(u64 &s) { return (double)(nextU64(s) >> 11) * (1.0 / 9007199254740992.0); }
+
+}  // namespace
+
+extern "C" void fcdemSceneLattice(float *pos4, float *vel4, uint n, float radius,
+                                  float spacing, float jitter, float velRange,
+                                  unsigned long long seed) {
+  u64 s = seed;
+  uint side = (uint)std::ceil(std::pow((double)n, 1.0 / 3.0));
+  while ((uint64_t)side * side * side < n) ++side;
+  uint i = 0;
+  for (uint z = 0; z < side && i < n; ++z)
+    for (uint y = 0; y < side && i < n; ++y)
+      for (uint x = 0; x < side && i < n; ++x, ++i) {
+        float c[3] = {(float)x, (float)y, (float)z};
+        for (int k = 0; k < 3; ++k)
+          pos4[4 * (size_t)i + k] =
+              (spacing * c[k]) + radius - 1.0f + (uniformF(s) * 2.0f - 1.0f) * jitter;
+        pos4[4 * (size_t)i + 3] = 1.0f;
+        for (int k = 0; k < 3; ++k)
+          vel4[4 * (size_t)i + k] = (uniformF(s) * 2.0f - 1.0f) * velRange;
+        vel4[4 * (size_t)i + 3] = 0.0f;
+      }
+}
+
+extern "C" uint fcdemScenePack(float *pos4, float *vel4, uint n, const float boxMin[3],
+                               const float boxMax[3], float rMedian, float sigma,
+                               float rMax, float velRange, unsigned long long seed,
+                               uint maxAttempts) {
+  u64 s = seed;
+  std::vector<float> radii(n);
+  for (uint i = 0; i < n; ++i) {
+    // Box-Muller normal, then lognormal around the median.
+    double u1 = uniformD(s), u2 = uniformD(s);
+    if (u1 < 1e-300) u1 = 1e-300;
+    double z = std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+    double r = (double)rMedian * std::exp((double)sigma * z);
+    radii[i] = (float)std::min(r, (double)rMax);
+  }
+  // The box is filled slab by slab along z, each slab at least 8 rMax thick
+  // and given a share of the spheres proportional to the height its centres
+  // can use, largest first; a candidate is then tested only against spheres
+  // that are still in cache.  Centres of a slab lie inside it; its spheres
+  // may reach into the previous slab and are tested against it.
+  const float height = boxMax[2] - boxMin[2];
+  uint slabs = (uint)std::max(1.0f, std::floor(height / (8.0f * rMax)));
+  slabs = std::max(1u, std::min(slabs, n / 4096u + 1u));
+  const float zs = height / (float)slabs;
+  std::vector<double> weight(slabs);
+  double wsum = 0.0;
+  for (uint k = 0; k < slabs; ++k) {
+    double lo = std::max((double)boxMin[2] + zs * k, (double)boxMin[2] + rMedian);
+    double hi = std::min((double)boxMin[2] + zs * (k + 1), (double)boxMax[2] - rMedian);
+    weight[k] = std::max(0.0, hi - lo);
+    wsum += weight[k];
+  }
+  std::vector<size_t> first(slabs + 1, 0);
+  double acc = 0.0;
+  for (uint k = 0; k < slabs; ++k) {
+    acc += weight[k];
+    first[k + 1] = (k + 1 == slabs) ? n : (size_t)std::llround(acc / wsum * n);
+  }
+  for (uint k = 0; k < slabs; ++k)
+    std::sort(radii.begin() + first[k], radii.begin() + first[k + 1],
+              [](float a, float c) { return a > c; });
+
+  // Occupancy grid with cell = 2 rMax: overlaps of a candidate are among the
+  // 27 cells around it.
+  const float cell = 2.0f * rMax;
+  int dims[3];
+  for (int k = 0; k < 3; ++k)
+    dims[k] = std::max(1, (int)std::ceil((boxMax[k] - boxMin[k]) / cell));
+  const size_t ncell = (size_t)dims[0] * dims[1] * dims[2];
+  std::vector<int> head(ncell, -1), next(n, -1);
+  auto cellOf = [&](const float p[3], int c[3]) {
+    for (int k = 0; k < 3; ++k) {
+      int v = (int)std::floor((p[k] - boxMin[k]) / cell);
+      c[k] = std::min(std::max(v, 0), dims[k] - 1);
+    }
+  };
+  uint placed = 0;
+  for (uint i = 0; i < n; ++i) {
+    const float r = radii[i];
+    uint slab = 0;
+    while (slab + 1 < slabs && i >= first[slab + 1]) ++slab;
+    float zlo = std::max(boxMin[2] + r, boxMin[2] + zs * (float)slab);
+    float zhi = std::min(boxMax[2] - r, boxMin[2] + zs * (float)(slab + 1));
+    if (zhi < zlo) zhi = zlo;
+    bool ok = false;
+    float p[3];
+    for (uint a = 0; a < maxAttempts && !ok; ++a) {
+      for (int k = 0; k < 2; ++k) {
+        float lo = boxMin[k] + r, hi = boxMax[k] - r;
+        p[k] = lo + uniformF(s) * (hi - lo);
+      }
+      p[2] = zlo + uniformF(s) * (zhi - zlo);
+      int c[3];
+      cellOf(p, c);
+      ok = true;
+      for (int dz = -1; dz <= 1 && ok; ++dz)
+        for (int dy = -1; dy <= 1 && ok; ++dy)
+          for (int dx = -1; dx <= 1 && ok; ++dx) {
+            int x = c[0] + dx, y = c[1] + dy, z = c[2] + dz;
+            if (x < 0 || y < 0 || z < 0 || x >= dims[0] || y >= dims[1] || z >= dims[2])
+              continue;
+            for (int j = head[((size_t)z * dims[1] + y) * dims[0] + x]; j >= 0; j = next[j]) {
+              const float *q = pos4 + 4 * (size_t)j;
+              float ex = q[0] - p[0], ey = q[1] - p[1], ez = q[2] - p[2];
+              float rr = q[3] + r;
+              if (ex * ex + ey * ey + ez * ez < rr * rr) { ok = false; break; }
+            }
+          }
+    }
+    if (!ok) break;
+    float *o = pos4 + 4 * (size_t)i;
+    o[0] = p[0]; o[1] = p[1]; o[2] = p[2]; o[3] = r;
+    for (int k = 0; k < 3; ++k) vel4[4 * (size_t)i + k] = (uniformF(s) * 2.0f - 1.0f) * velRange;
+    vel4[4 * (size_t)i + 3] = 0.0f;
+    int c[3];
+    cellOf(p, c);
+    size_t ci = ((size_t)c[2] * dims[1] + c[1]) * dims[0] + c[0];
+    next[i] = head[ci];
+    head[ci] = (int)i;
+    placed = i + 1;
+  }
+  return placed;
+}
+
+// ---------------------------------------------------------------------------
+namespace fcdem {
+
+ParticleSystem::ParticleSystem(uint numParticles, const uint gridSize[3], bool bUseOpenGL)
+    : m_hPos(nullptr), m_hVel(nullptr), m_bInitialized(false), m_bUseOpenGL(false),
+      m_fused(true), m_radiusFromW(false), m_numParticles(numParticles),
+      m_hCellStart(nullptr), m_hCellEnd(nullptr), m_dPos(nullptr), m_dVel(nullptr),
+      m_dSortedPos(nullptr), m_dSortedVel(nullptr), m_dGridParticleHash(nullptr),
+      m_dGridParticleIndex(nullptr), m_dCellStart(nullptr), m_dCellEnd(nullptr),
+      m_solverIterations(1), m_rng(1973) {
+  if (bUseOpenGL) registerGLBufferObject(0, nullptr);  // records UNSUPPORTED
+  for (int k = 0; k < 3; ++k) m_gridSize[k] = gridSize[k];
+  m_numGridCells = m_gridSize[0] * m_gridSize[1] * m_gridSize[2];
+  std::memset(&m_params, 0, sizeof(m_params));
+  // particleSystem.cpp:36-70
+  for (int k = 0; k < 3; ++k) m_params.gridSize[k] = m_gridSize[k];
+  m_params.numCells = m_numGridCells;
+  m_params.numBodies = m_numParticles;
+  m_params.particleRadius = 1.0f / 16.0f;
+  m_params.colliderPos[0] = -1.2f;
+  m_params.colliderPos[1] = -0.8f;
+  m_params.colliderPos[2] = 0.8f;
+  m_params.colliderRadius = 0.2f;
+  for (int k = 0; k < 3; ++k) m_params.worldOrigin[k] = -1.0f;
+  float cellSize = m_params.particleRadius * 2.0f;
+  for (int k = 0; k < 3; ++k) m_params.cellSize[k] = cellSize;
+  m_params.spring = 0.5f;
+  m_params.damping = 0.02f;
+  m_params.shear = 0.1f;
+  m_params.attraction = 0.0f;
+  m_params.boundaryDamping = -0.5f;
+  m_params.gravity[0] = 0.0f;
+  m_params.gravity[1] = 0.0f;
+  m_params.gravity[2] = -0.0003f;
+  m_params.globalDamping = 1.0f;
+  _initialize((int)numParticles);
+}
+
+ParticleSystem::~ParticleSystem() {
+  _finalize();
+  m_numParticles = 0;
+}
+
+void ParticleSystem::_initialize(int numParticles) {
+  m_numParticles = (uint)numParticles;
+  size_t n4 = (size_t)m_numParticles * 4;
+  m_hPos = new float[n4]();
+  m_hVel = new float[n4]();
+  m_hCellStart = new uint[m_numGridCells]();
+  m_hCellEnd = new uint[m_numGridCells]();
+  size_t memSize = sizeof(float) * n4;
+  allocateArray((void **)&m_dPos, memSize);
+  allocateArray((void **)&m_dVel, memSize);
+  allocateArray((void **)&m_dSortedPos, memSize);
+  allocateArray((void **)&m_dSortedVel, memSize);
+  allocateArray((void **)&m_dGridParticleHash, m_numParticles * sizeof(uint));
+  allocateArray((void **)&m_dGridParticleIndex, m_numParticles * sizeof(uint));
+  allocateArray((void **)&m_dCellStart, m_numGridCells * sizeof(uint));
+  allocateArray((void **)&m_dCellEnd, m_numGridCells * sizeof(uint));
+  setParameters(&m_params);
+  m_bInitialized = true;
+}
+
+void ParticleSystem::_finalize() {
+  if (!m_bInitialized) return;
+  delete[] m_hPos;
+  delete[] m_hVel;
+  delete[] m_hCellStart;
+  delete[] m_hCellEnd;
+  freeArray(m_dPos);
+  freeArray(m_dVel);
+  freeArray(m_dSortedPos);
+  freeArray(m_dSortedVel);
+  freeArray(m_dGridParticleHash);
+  freeArray(m_dGridParticleIndex);
+  freeArray(m_dCellStart);
+  freeArray(m_dCellEnd);
+  m_bInitialized = false;
+}
+
+void ParticleSystem::update(float deltaTime) { updateSteps(deltaTime, 1); }
+
+void ParticleSystem::updateSteps(float deltaTime, uint steps) {
+  if (!m_bInitialized || steps == 0) return;
+  setParameters(&m_params);
+  fcdemSetRadiusMode(m_radiusFromW ? 1 : 0);
+  if (m_fused) {
+    fcdemUpdate(m_dPos, m_dVel, m_dSortedPos, m_dSortedVel, m_dGridParticleHash,
+                m_dGridParticleIndex, m_dCellStart, m_dCellEnd, deltaTime,
+                m_numParticles, m_numGridCells, steps);
+    return;
+  }
+  for (uint s = 0; s < steps; ++s) {  // particleSystem.cpp:236-281
+    integrateSystem(m_dPos, m_dVel, deltaTime, m_numParticles);
+    calcHash(m_dGridParticleHash, m_dGridParticleIndex, m_dPos, (int)m_numParticles);
+    sortParticles(m_dGridParticleHash, m_dGridParticleIndex, m_numParticles);
+    reorderDataAndFindCellStart(m_dCellStart, m_dCellEnd, m_dSortedPos, m_dSortedVel,
+                                m_dGridParticleHash, m_dGridParticleIndex, m_dPos,
+                                m_dVel, m_numParticles, m_numGridCells);
+    collide(m_dVel, m_dSortedPos, m_dSortedVel, m_dGridParticleIndex, m_dCellStart,
+            m_dCellEnd, m_numParticles, m_numGridCells);
+  }
+}
+
+uint ParticleSystem::dumpGrid() {
+  copyArrayFromDevice(m_hCellStart, m_dCellStart, nullptr, (int)(sizeof(uint) * m_numGridCells));
+  copyArrayFromDevice(m_hCellEnd, m_dCellEnd, nullptr, (int)(sizeof(uint) * m_numGridCells));
+  uint maxCellSize = 0;
+  for (uint i = 0; i < m_numGridCells; i++)
+    if (m_hCellStart[i] != 0xffffffffu)
+      maxCellSize = std::max(maxCellSize, m_hCellEnd[i] - m_hCellStart[i]);
+  return maxCellSize;
+}
+
+void ParticleSystem::transferArrays(uint start, uint count) {
+  (void)start;
+  copyArrayFromDevice(m_hPos, m_dPos, nullptr, (int)(sizeof(float) * 4 * count));
+  copyArrayFromDevice(m_hVel, m_dVel, nullptr, (int)(sizeof(float) * 4 * count));
+}
+
+float *ParticleSystem::getArray(ParticleArray array) {
+  float *h = array == VELOCITY ? m_hVel : m_hPos;
+  float *d = array == VELOCITY ? m_dVel : m_dPos;
+  copyArrayFromDevice(h, d, nullptr, (int)(m_numParticles * 4 * sizeof(float)));
+  return h;
+}
+
+void ParticleSystem::setArray(ParticleArray array, const float *data, int start, int count) {
+  float *d = array == VELOCITY ? m_dVel : m_dPos;
+  copyArrayToDevice(d, data, start * 4 * (int)sizeof(float), count * 4 * (int)sizeof(float));
+}
+
+float ParticleSystem::frand() { return uniformF(m_rng); }
+
+void ParticleSystem::initGrid(const uint size[3], float spacing, float jitter,
+                              uint numParticles) {  // particleSystem.cpp:380-402
+  for (uint z = 0; z < size[2]; z++)
+    for (uint y = 0; y < size[1]; y++)
+      for (uint x = 0; x < size[0]; x++) {
+        uint i = (z * size[1] * size[0]) + (y * size[0]) + x;
+        if (i < numParticles) {
+          m_hPos[i * 4] = (spacing * x) + m_params.particleRadius - 1.0f + (frand() * 2.0f - 1.0f) * jitter;
+          m_hPos[i * 4 + 1] = (spacing * y) + m_params.particleRadius - 1.0f + (frand() * 2.0f - 1.0f) * jitter;
+          m_hPos[i * 4 + 2] = (spacing * z) + m_params.particleRadius - 1.0f + (frand() * 2.0f - 1.0f) * jitter;
+          m_hPos[i * 4 + 3] = 1.0f;
+          m_hVel[i * 4] = m_hVel[i * 4 + 1] = m_hVel[i * 4 + 2] = m_hVel[i * 4 + 3] = 0.0f;
+        }
+      }
+}
+
+void ParticleSystem::reset(ParticleConfig config) {  // particleSystem.cpp:404-444
+  m_rng = 1973;
+  if (config == CONFIG_GRID) {
+    float jitter = m_params.particleRadius * 0.01f;
+    uint s = (uint)std::ceil(std::pow((float)m_numParticles, 1.0f / 3.0f));
+    uint gs[3] = {s, s, s};
+    initGrid(gs, m_params.particleRadius * 2.0f, jitter, m_numParticles);
+  } else {
+    size_t p = 0, v = 0;
+    for (uint i = 0; i < m_numParticles; i++) {
+      float pt[3] = {frand(), frand(), frand()};
+      m_hPos[p++] = 2 * (pt[0] - 0.5f);
+      m_hPos[p++] = 2 * (pt[1] - 0.5f);
+      m_hPos[p++] = 2 * (pt[2] - 0.5f);
+      m_hPos[p++] = 1.0f;
+      m_hVel[v++] = 0.0f; m_hVel[v++] = 0.0f; m_hVel[v++] = 0.0f; m_hVel[v++] = 0.0f;
+    }
+  }
+  setArray(POSITION, m_hPos, 0, (int)m_numParticles);
+  setArray(VELOCITY, m_hVel, 0, (int)m_numParticles);
+}
+
+void ParticleSystem::setParticles(const float *positions, const float *velocities) {
+  for (uint i = 0; i < m_numParticles; i++) {
+    for (int k = 0; k < 3; ++k) {
+      m_hPos[i * 4 + k] = positions[i * 4 + k];
+      m_hVel[i * 4 + k] = velocities[i * 4 + k];
+    }
+    m_hPos[i * 4 + 3] = m_radiusFromW ? positions[i * 4 + 3] : 1.0f;
+    m_hVel[i * 4 + 3] = 0.0f;
+  }
+  setArray(POSITION, m_hPos, 0, (int)m_numParticles);
+  setArray(VELOCITY, m_hVel, 0, (int)m_numParticles);
+}
+
+void ParticleSystem::setVelocity(const float *velocities) {
+  for (uint i = 0; i < m_numParticles; i++) {
+    for (int k = 0; k < 3; ++k) m_hVel[i * 4 + k] = velocities[i * 4 + k];
+    m_hVel[i * 4 + 3] = 0.0f;
+  }
+  setArray(VELOCITY, m_hVel, 0, (int)m_numParticles);
+}
+
+void ParticleSystem::addSphere(int start, const float *pos, const float *vel, int r,
+                               float spacing) {  // particleSystem.cpp:617-647
+  uint index = (uint)start;
+  for (int z = -r; z <= r; z++)
+    for (int y = -r; y <= r; y++)
+      for (int x = -r; x <= r; x++) {
+        float dx = x * spacing, dy = y * spacing, dz = z * spacing;
+        float l = std::sqrt(dx * dx + dy * dy + dz * dz);
+        float jitter = m_params.particleRadius * 0.01f;
+        if ((l <= m_params.particleRadius * 2.0f * r) && (index < m_numParticles)) {
+          m_hPos[index * 4] = pos[0] + dx + (frand() * 2.0f - 1.0f) * jitter;
+          m_hPos[index * 4 + 1] = pos[1] + dy + (frand() * 2.0f - 1.0f) * jitter;
+          m_hPos[index * 4 + 2] = pos[2] + dz + (frand() * 2.0f - 1.0f) * jitter;
+          m_hPos[index * 4 + 3] = pos[3];
+          for (int k = 0; k < 4; ++k) m_hVel[index * 4 + k] = vel[k];
+          index++;
+        }
+      }
+  setArray(POSITION, m_hPos + 4 * (size_t)start, start, (int)(index - (uint)start));
+  setArray(VELOCITY, m_hVel + 4 * (size_t)start, start, (int)(index - (uint)start));
+}
+
+}  // namespace fcdem
+
+// ---------------------------------------------------------------------------
+struct fcdemParticleSystem {
+  fcdem::ParticleSystem ps;
+  fcdemParticleSystem(uint n, const uint g[3]) : ps(n, g, false) {}
+};
+
+extern "C" {
+
+fcdemParticleSystem *fcdemPS_create(uint numParticles, uint gx, uint gy, uint gz) {
+  uint g[3] = {gx, gy, gz};
+  return new fcdemParticleSystem(numParticles, g);
+}
+void fcdemPS_destroy(fcdemParticleSystem *ps) { delete ps; }
+SimParams *fcdemPS_params(fcdemParticleSystem *ps) { return &ps->ps.params(); }
+void fcdemPS_update(fcdemParticleSystem *ps, float dt) { ps->ps.update(dt); }
+void fcdemPS_updateSteps(fcdemParticleSystem *ps, float dt, uint steps) {
+  ps->ps.updateSteps(dt, steps);
+}
+void fcdemPS_reset(fcdemParticleSystem *ps, int config) {
+  ps->ps.reset(config == 1 ? fcdem::ParticleSystem::CONFIG_GRID
+                           : fcdem::ParticleSystem::CONFIG_RANDOM);
+}
+void fcdemPS_setArray(fcdemParticleSystem *ps, int array, const float *data, int start,
+                      int count) {
+  ps->ps.setArray(array == 1 ? fcdem::ParticleSystem::VELOCITY
+                             : fcdem::ParticleSystem::POSITION,
+                  data, start, count);
+}
+const float *fcdemPS_getArray(fcdemParticleSystem *ps, int array) {
+  return ps->ps.getArray(array == 1 ? fcdem::ParticleSystem::VELOCITY
+                                    : fcdem::ParticleSystem::POSITION);
+}
+uint fcdemPS_dumpGrid(fcdemParticleSystem *ps) { return ps->ps.dumpGrid(); }
+void fcdemPS_setFusedUpdate(fcdemParticleSystem *ps, int fused) {
+  ps->ps.setFusedUpdate(fused != 0);
+}
+void fcdemPS_setRadiusFromW(fcdemParticleSystem *ps, int on) {
+  ps->ps.setRadiusFromW(on != 0);
+}
+float *fcdemPS_devicePos(fcdemParticleSystem *ps) { return ps->ps.getDevicePos(); }
+float *fcdemPS_deviceVel(fcdemParticleSystem *ps) { return ps->ps.getDeviceVel(); }
+
+}  // extern "C"

@@ -1,0 +1,308 @@
+// fcdem_sort.cu -- stable LSD radix sort of (key, value) pairs: the stage
+// the reference hands to thrust::sort_by_key (particleSystem.cu:328-333).
+//
+// One upsweep kernel builds the digit histograms of every pass in one read of
+// the keys; then each pass is a single "onesweep" kernel: a CTA takes the
+// next tile (4096 keys) from an atomic counter, ranks its keys stably by
+// digit with warp ballots, publishes its per-digit counts, resolves its
+// global offsets by decoupled look-back over the tiles before it, stages the
+// tile in shared memory in digit order and writes it out in runs.
+//
+// Every look-back spin is bounded: after kSpinLimit polls the CTA records
+// kStatusTimeout in the device status word and carries on, so a fault in the
+// protocol turns into an error the host reads, never into a hung GPU.
+#include "fcdem_internal.cuh"
+
+namespace fcdem {
+namespace {
+
+constexpr int kRadixBits = 8;
+constexpr int kRadix = 1 << kRadixBits;
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kItems = 16;
+constexpr int kTile = kThreads * kItems;  // 4096 keys
+constexpr int kWarpKeys = 32 * kItems;    // 512 keys per warp
+constexpr int kMaxPasses = 4;
+constexpr unsigned kFlagAgg = 1u << 30;
+constexpr unsigned kFlagPrefix = 2u << 30;
+constexpr unsigned kValueMask = (1u << 30) - 1u;
+constexpr unsigned kSpinLimit = 1u << 22;
+
+static_assert(kThreads == kRadix, "one thread per digit in the scan phases");
+
+__device__ __forceinline__ unsigned lanemaskLt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Mask of the lanes of `active` whose digit equals this lane's (8 ballots).
+__device__ __forceinline__ unsigned digitPeers(unsigned d, unsigned active) {
+  unsigned peers = active;
+#pragma unroll
+  for (int b = 0; b < kRadixBits; ++b) {
+    unsigned bit = (d >> b) & 1u;
+    unsigned vote = __ballot_sync(0xffffffffu, bit);
+    peers &= bit ? vote : ~vote;
+  }
+  return peers;
+}
+
+__device__ __forceinline__ unsigned ldVolatile(const unsigned *p) {
+  return *(const volatile unsigned *)p;
+}
+__device__ __forceinline__ void stVolatile(unsigned *p, unsigned v) {
+  *(volatile unsigned *)p = v;
+}
+
+// Exclusive scan of one value per thread over a 256-thread block.
+__device__ __forceinline__ unsigned blockExclusiveScan(unsigned v,
+                                                       unsigned *warpSums) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warpSums[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    unsigned s = lane < kWarps ? warpSums[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < kWarps; o <<= 1) {
+      unsigned y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
+    }
+    if (lane < kWarps) warpSums[lane] = s;  // inclusive warp totals
+  }
+  __syncthreads();
+  unsigned before = warp ? warpSums[warp - 1] : 0u;
+  unsigned r = before + x - v;
+  __syncthreads();  // warpSums may be reused by the caller
+  return r;
+}
+
+// Histograms of all `passes` digits; checks that no key has bits at or above
+// `bits`.  hist must be zero on entry.
+__global__ void __launch_bounds__(kThreads)
+kUpsweep(const unsigned *__restrict__ keys, unsigned n, int passes, int bits,
+         unsigned *__restrict__ hist, unsigned *__restrict__ status) {
+  __shared__ unsigned sh[kMaxPasses][kRadix];
+  for (int k = threadIdx.x; k < kMaxPasses * kRadix; k += kThreads)
+    (&sh[0][0])[k] = 0;
+  __syncthreads();
+  const unsigned lt = lanemaskLt();
+  const unsigned lane = threadIdx.x & 31;
+  bool bad = false;
+  unsigned stride = gridDim.x * kThreads;
+  unsigned nRound = (n + 31u) & ~31u;
+  for (unsigned base = blockIdx.x * kThreads + (threadIdx.x & ~31u); base < nRound;
+       base += stride) {
+    unsigned i = base + lane;
+    bool valid = i < n;
+    unsigned k = valid ? __ldg(keys + i) : 0u;
+    if (valid && bits < 32 && (k >> bits) != 0u) bad = true;
+    unsigned active = __ballot_sync(0xffffffffu, valid);
+    for (int p = 0; p < passes; ++p) {
+      unsigned d = (k >> (p * kRadixBits)) & (kRadix - 1);
+      unsigned peers = digitPeers(d, active);
+      if (valid && (peers & lt) == 0u) atomicAdd(&sh[p][d], (unsigned)__popc(peers));
+    }
+  }
+  if (bad) atomicOr(status, (unsigned)kStatusKeyRange);
+  __syncthreads();
+  for (int p = 0; p < passes; ++p) {
+    unsigned c = sh[p][threadIdx.x];
+    if (c) atomicAdd(hist + p * kRadix + threadIdx.x, c);
+  }
+}
+
+// One counting pass over digit `shift`.  lookback has one kRadix-word row per
+// tile and must be zero on entry, as must *tileCounter.  valsIn == nullptr
+// stands for the identity values 0, 1, ..., n-1.
+__global__ void __launch_bounds__(kThreads, 2)
+kOnesweep(const unsigned *__restrict__ keysIn, const unsigned *__restrict__ valsIn,
+          unsigned *__restrict__ keysOut, unsigned *__restrict__ valsOut,
+          unsigned n, int shift, const unsigned *__restrict__ hist,
+          unsigned *lookback, unsigned *tileCounter, unsigned *status) {
+  __shared__ unsigned sTile;
+  __shared__ unsigned sWarpHist[kWarps][kRadix];
+  __shared__ unsigned sBinExcl[kRadix];
+  __shared__ int sBase[kRadix];
+  __shared__ unsigned sWarpSums[kWarps];
+  __shared__ unsigned sKeys[kTile];
+  __shared__ unsigned sVals[kTile];
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) sTile = atomicAdd(tileCounter, 1u);
+  for (int k = tid; k < kWarps * kRadix; k += kThreads) (&sWarpHist[0][0])[k] = 0;
+  __syncthreads();
+  const unsigned tile = sTile;
+  const unsigned base = tile * (unsigned)kTile;
+  const unsigned wbase = base + warp * kWarpKeys;
+
+  unsigned key[kItems], val[kItems], rank[kItems];
+#pragma unroll
+  for (int r = 0; r < kItems; ++r) {
+    unsigned idx = wbase + r * 32 + lane;
+    bool valid = idx < n;
+    key[r] = valid ? __ldg(keysIn + idx) : 0u;
+    val[r] = valid ? (valsIn ? __ldg(valsIn + idx) : idx) : 0u;
+  }
+
+  // Stable rank inside the warp: rounds in position order, lanes in position
+  // order within a round.
+  const unsigned lt = lanemaskLt();
+#pragma unroll
+  for (int r = 0; r < kItems; ++r) {
+    unsigned idx = wbase + r * 32 + lane;
+    bool valid = idx < n;
+    unsigned active = __ballot_sync(0xffffffffu, valid);
+    unsigned d = (key[r] >> shift) & (kRadix - 1);
+    unsigned peers = digitPeers(d, active);
+    unsigned before = valid ? sWarpHist[warp][d] : 0u;
+    __syncwarp();
+    if (valid && (peers & lt) == 0u) sWarpHist[warp][d] = before + __popc(peers);
+    __syncwarp();
+    rank[r] = before + __popc(peers & lt);
+  }
+  __syncthreads();
+
+  // Thread b owns digit b: per-warp exclusive offsets and the tile count.
+  const unsigned b = tid;
+  unsigned count = 0;
+#pragma unroll
+  for (int w = 0; w < kWarps; ++w) {
+    unsigned c = sWarpHist[w][b];
+    sWarpHist[w][b] = count;
+    count += c;
+  }
+
+  // Decoupled look-back over the tiles before this one.
+  unsigned *row = lookback + (size_t)tile * kRadix;
+  unsigned excl = 0;
+  if (tile == 0) {
+    stVolatile(row + b, kFlagPrefix | count);
+  } else {
+    stVolatile(row + b, kFlagAgg | count);
+    int t = (int)tile - 1;
+    unsigned spins = 0;
+    while (t >= 0) {
+      unsigned w = ldVolatile(lookback + (size_t)t * kRadix + b);
+      unsigned flag = w & ~kValueMask;
+      if (flag == 0u) {
+        if (++spins > kSpinLimit) {
+          atomicOr(status, (unsigned)kStatusTimeout);
+          break;
+        }
+        if (spins > 64) __nanosleep(64);
+        continue;
+      }
+      excl += w & kValueMask;
+      if (flag == kFlagPrefix) break;
+      --t;
+    }
+    stVolatile(row + b, kFlagPrefix | ((excl + count) & kValueMask));
+  }
+
+  unsigned digitStart = blockExclusiveScan(__ldg(hist + b), sWarpSums);
+  unsigned binExcl = blockExclusiveScan(count, sWarpSums);
+  sBinExcl[b] = binExcl;
+  sBase[b] = (int)(digitStart + excl) - (int)binExcl;
+  __syncthreads();
+
+  // Stage the tile in digit order.
+#pragma unroll
+  for (int r = 0; r < kItems; ++r) {
+    unsigned idx = wbase + r * 32 + lane;
+    if (idx < n) {
+      unsigned d = (key[r] >> shift) & (kRadix - 1);
+      unsigned lp = sBinExcl[d] + sWarpHist[warp][d] + rank[r];
+      sKeys[lp] = key[r];
+      sVals[lp] = val[r];
+    }
+  }
+  __syncthreads();
+
+  // Write out: consecutive staged slots of one digit go to consecutive
+  // global positions.
+  unsigned tileCount = n - base < (unsigned)kTile ? n - base : (unsigned)kTile;
+#pragma unroll
+  for (int r = 0; r < kItems; ++r) {
+    unsigned lp = r * kThreads + tid;
+    if (lp < tileCount) {
+      unsigned k = sKeys[lp];
+      unsigned d = (k >> shift) & (kRadix - 1);
+      unsigned g = (unsigned)(sBase[d] + (int)lp);
+      keysOut[g] = k;
+      valsOut[g] = sVals[lp];
+    }
+  }
+}
+
+inline size_t alignUp(size_t v) { return (v + 255) & ~(size_t)255; }
+
+}  // namespace
+
+void radixSortPairs(Context &c, unsigned *keys, unsigned *vals, unsigned n,
+                    int bits, bool identityVals) {
+  if (n < 2) return;
+  if (n > kValueMask) { setError(FCDEM_ERR_INVALID_VALUE); return; }
+  if (bits < 1) bits = 1;
+  if (bits > 32) bits = 32;
+  const int passes = (bits + kRadixBits - 1) / kRadixBits;
+  const unsigned tiles = (n + kTile - 1) / kTile;
+  const size_t arr = alignUp((size_t)n * 4);
+  const size_t histBytes = alignUp(kMaxPasses * kRadix * 4 + kMaxPasses * 4);
+  const size_t lbBytes = alignUp((size_t)passes * tiles * kRadix * 4);
+  const int buffers = (passes % 2 == 1) ? 2 : 1;  // extra key/value pairs
+  const size_t total = (size_t)buffers * 2 * arr + histBytes + lbBytes;
+  char *s = (char *)scratch(c, total);
+  if (!s) return;
+  unsigned *kB = (unsigned *)s, *vB = (unsigned *)(s + arr);
+  unsigned *kC = buffers > 1 ? (unsigned *)(s + 2 * arr) : nullptr;
+  unsigned *vC = buffers > 1 ? (unsigned *)(s + 3 * arr) : nullptr;
+  char *meta = s + (size_t)buffers * 2 * arr;
+  unsigned *hist = (unsigned *)meta;
+  unsigned *counters = hist + kMaxPasses * kRadix;
+  unsigned *lookback = (unsigned *)(meta + histBytes);
+  cudaStream_t st = curStream();
+
+  if (!cudaOk(cudaMemsetAsync(meta, 0, histBytes + lbBytes, st))) return;
+  unsigned upBlocks = (n + kThreads * 16 - 1) / (kThreads * 16);
+  if (upBlocks > 152u * 4u) upBlocks = 152u * 4u;
+  kUpsweep<<<upBlocks, kThreads, 0, st>>>(keys, n, passes, bits, hist, c.dStatus);
+  if (!launchOk()) return;
+
+  // Buffer routing: even pass counts alternate A->B->A; odd counts >= 3 go
+  // A->B->C->A first so that the result lands in the caller's arrays.
+  unsigned *srcK = keys, *srcV = identityVals ? nullptr : vals;
+  for (int p = 0; p < passes; ++p) {
+    unsigned *dstK, *dstV;
+    if (passes == 1) {
+      dstK = kB; dstV = vB;
+    } else if (passes % 2 == 1 && p < 3) {
+      if (p == 0) { dstK = kB; dstV = vB; }
+      else if (p == 1) { dstK = kC; dstV = vC; }
+      else { dstK = keys; dstV = vals; }
+    } else {
+      bool toB = (srcK == keys);
+      dstK = toB ? kB : keys;
+      dstV = toB ? vB : vals;
+    }
+    kOnesweep<<<tiles, kThreads, 0, st>>>(
+        srcK, srcV, dstK, dstV, n, p * kRadixBits, hist + p * kRadix,
+        lookback + (size_t)p * tiles * kRadix, counters + p, c.dStatus);
+    if (!launchOk()) return;
+    srcK = dstK;
+    srcV = dstV;
+  }
+  if (srcK != keys) {  // single pass: copy back
+    cudaOk(cudaMemcpyAsync(keys, srcK, (size_t)n * 4, cudaMemcpyDeviceToDevice, st));
+    cudaOk(cudaMemcpyAsync(vals, srcV, (size_t)n * 4, cudaMemcpyDeviceToDevice, st));
+  }
+}
+
+}  // namespace fcdem

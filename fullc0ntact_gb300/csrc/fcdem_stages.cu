@@ -1,0 +1,404 @@
+// fcdem_stages.cu -- integrate, hash, reorder and collide kernels and the
+// reference-named entry points that launch them
+// (particleSystem.cu:204-325, particles_kernel.cu:39-293).
+#include "fcdem_dem.cuh"
+
+namespace fcdem {
+
+constexpr unsigned kEmpty = 0xffffffffu;
+
+// ---------------------------------------------------------------------------
+// integrate (particles_kernel.cu:39-75; launched by thrust::for_each in
+// particleSystem.cu:204-216).  One thread per particle, 128-bit loads/stores.
+__global__ void __launch_bounds__(256)
+kIntegrate(float4 *__restrict__ pos, float4 *__restrict__ vel, float dt,
+           unsigned n, KParams kp) {
+  unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 p4 = pos[i], v4 = vel[i];
+  float3 p = make_float3(p4.x, p4.y, p4.z), v = make_float3(v4.x, v4.y, v4.z);
+  float r = kp.radiusFromW ? p4.w : kp.p.particleRadius;
+  integrateOne(p, v, dt, r, kp.p);
+  pos[i] = make_float4(p.x, p.y, p.z, p4.w);
+  vel[i] = make_float4(v.x, v.y, v.z, v4.w);
+}
+
+// ---------------------------------------------------------------------------
+// calcHash (particles_kernel.cu:97-115).
+__global__ void __launch_bounds__(256)
+kCalcHash(unsigned *__restrict__ hash, unsigned *__restrict__ index,
+          const float4 *__restrict__ pos, unsigned n, KParams kp) {
+  unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 p = ldg4(pos + i);
+  int3 g = gridPos(p.x, p.y, p.z, kp.p);
+  hash[i] = gridHash(g.x, g.y, g.z, kp.p);
+  index[i] = i;
+}
+
+// integrate + calcHash in one pass (the first two stages of
+// ParticleSystem::update, particleSystem.cpp:239-251).
+__global__ void __launch_bounds__(256)
+kIntegrateHash(float4 *__restrict__ pos, float4 *__restrict__ vel, float dt,
+               unsigned *__restrict__ hash, unsigned *__restrict__ index,
+               unsigned n, KParams kp) {
+  unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 p4 = pos[i], v4 = vel[i];
+  float3 p = make_float3(p4.x, p4.y, p4.z), v = make_float3(v4.x, v4.y, v4.z);
+  float r = kp.radiusFromW ? p4.w : kp.p.particleRadius;
+  integrateOne(p, v, dt, r, kp.p);
+  pos[i] = make_float4(p.x, p.y, p.z, p4.w);
+  vel[i] = make_float4(v.x, v.y, v.z, v4.w);
+  int3 g = gridPos(p.x, p.y, p.z, kp.p);
+  hash[i] = gridHash(g.x, g.y, g.z, kp.p);
+  index[i] = i;
+}
+
+// ---------------------------------------------------------------------------
+// Fill (the cudaMemset of particleSystem.cu:261).  16-byte stores where the
+// pointer allows, grid-stride.
+__global__ void __launch_bounds__(256)
+kFill(unsigned *__restrict__ p, size_t count, unsigned value) {
+  size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t stride = (size_t)gridDim.x * blockDim.x;
+  size_t head = (16u - ((uintptr_t)p & 15u)) / 4u & 3u;
+  if (head > count) head = count;
+  if (tid < head) p[tid] = value;
+  size_t n4 = (count - head) / 4;
+  uint4 *q = reinterpret_cast<uint4 *>(p + head);
+  uint4 v = make_uint4(value, value, value, value);
+  for (size_t k = tid; k < n4; k += stride) q[k] = v;
+  size_t tail = head + n4 * 4;
+  if (tid < count - tail) p[tail + tid] = value;
+}
+
+void fillU32(Context &, unsigned *p, size_t count, unsigned value) {
+  if (count == 0) return;
+  size_t work = (count + 3) / 4;
+  unsigned blocks = (unsigned)((work + 255) / 256);
+  if (blocks > 152u * 16u) blocks = 152u * 16u;
+  if (blocks == 0) blocks = 1;
+  kFill<<<blocks, 256, 0, curStream()>>>(p, count, value);
+  launchOk();
+}
+
+// ---------------------------------------------------------------------------
+// reorderDataAndFindCellStart (particles_kernel.cu:119-182).  The previous
+// hash is read directly (adjacent threads share the cache line), the gathers
+// are 128-bit.
+__global__ void __launch_bounds__(256)
+kReorder(unsigned *__restrict__ cellStart, unsigned *__restrict__ cellEnd,
+         float4 *__restrict__ sortedPos, float4 *__restrict__ sortedVel,
+         const unsigned *__restrict__ hash, const unsigned *__restrict__ index,
+         const float4 *__restrict__ oldPos, const float4 *__restrict__ oldVel,
+         unsigned n) {
+  unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  unsigned h = __ldg(hash + i);
+  if (i == 0) {
+    cellStart[h] = 0;
+  } else {
+    unsigned hp = __ldg(hash + i - 1);
+    if (h != hp) {
+      cellStart[h] = i;
+      cellEnd[hp] = i;
+    }
+  }
+  if (i == n - 1) cellEnd[h] = n;
+  unsigned s = __ldg(index + i);
+  sortedPos[i] = ldg4(oldPos + s);
+  sortedVel[i] = ldg4(oldVel + s);
+}
+
+// ---------------------------------------------------------------------------
+// collide (particles_kernel.cu:185-293).  One thread per sorted particle.
+// The neighbour cells are visited in the reference's z, y, x order and the
+// particles of a cell in ascending sorted index; each cell's terms are summed
+// into a cell subtotal that is then added to the particle total, as
+// collideCell/collideD do, so the float sums are the reference's.  The
+// neighbour's velocity is only loaded for pairs in contact.
+//
+// kMode 0: write newVel[index[i]] = (v + F, 0) (the reference).
+// kMode 1: additionally integrate the particle for the next step and write
+//          pos/vel/hash/index of the next step (fcdemUpdate).
+template <int kMode, bool kRadiusFromW, bool kCollider, bool kForceOut>
+__global__ void __launch_bounds__(128)
+kCollide(float4 *__restrict__ newVel, float3 *__restrict__ forceOut,
+         const float4 *__restrict__ sortedPos,
+         const float4 *__restrict__ sortedVel,
+         const unsigned *__restrict__ index,
+         const unsigned *__restrict__ cellStart,
+         const unsigned *__restrict__ cellEnd, unsigned n, KParams kp,
+         float4 *__restrict__ posOut, unsigned *__restrict__ hashOut, float dt) {
+  const SimParams &P = kp.p;
+  unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 p4 = ldg4(sortedPos + i);
+  float4 v4 = ldg4(sortedVel + i);
+  float3 pos = make_float3(p4.x, p4.y, p4.z);
+  float3 vel = make_float3(v4.x, v4.y, v4.z);
+  float ri = kRadiusFromW ? p4.w : P.particleRadius;
+  int3 g = gridPos(pos.x, pos.y, pos.z, P);
+
+  float3 force = make_float3(0.0f, 0.0f, 0.0f);
+#pragma unroll 1
+  for (int z = -1; z <= 1; z++) {
+#pragma unroll 1
+    for (int y = -1; y <= 1; y++) {
+#pragma unroll
+      for (int x = -1; x <= 1; x++) {
+        unsigned h = gridHash(g.x + x, g.y + y, g.z + z, P);
+        unsigned start = __ldg(cellStart + h);
+        float3 cf = make_float3(0.0f, 0.0f, 0.0f);
+        if (start != kEmpty) {
+          unsigned end = __ldg(cellEnd + h);
+          for (unsigned j = start; j < end; j++) {
+            if (j == i) continue;
+            float4 q4 = ldg4(sortedPos + j);
+            float3 rel = make_float3(q4.x - pos.x, q4.y - pos.y, q4.z - pos.z);
+            float dist = pairDist(rel);
+            float cd = ri + (kRadiusFromW ? q4.w : P.particleRadius);
+            if (dist < cd) {
+              float4 w4 = ldg4(sortedVel + j);
+              float3 f = contactTerm(rel, dist, cd, vel,
+                                     make_float3(w4.x, w4.y, w4.z),
+                                     P.attraction, P);
+              cf.x = cf.x + f.x;
+              cf.y = cf.y + f.y;
+              cf.z = cf.z + f.z;
+            }
+          }
+        }
+        force.x = force.x + cf.x;
+        force.y = force.y + cf.y;
+        force.z = force.z + cf.z;
+      }
+    }
+  }
+  if (kCollider) {  // particles_kernel.cu:288, the collider sphere
+    float3 cpos = make_float3(P.colliderPos[0], P.colliderPos[1], P.colliderPos[2]);
+    float3 rel = make_float3(cpos.x - pos.x, cpos.y - pos.y, cpos.z - pos.z);
+    float dist = pairDist(rel);
+    float cd = ri + P.colliderRadius;
+    if (dist < cd) {
+      float3 f = contactTerm(rel, dist, cd, vel, make_float3(0.0f, 0.0f, 0.0f),
+                             0.0f, P);
+      force.x = force.x + f.x;
+      force.y = force.y + f.y;
+      force.z = force.z + f.z;
+    }
+  }
+  unsigned o = __ldg(index + i);
+  float3 nv = make_float3(vel.x + force.x, vel.y + force.y, vel.z + force.z);
+  if (kForceOut) forceOut[o] = force;
+  if (kMode == 0) {
+    newVel[o] = make_float4(nv.x, nv.y, nv.z, 0.0f);
+  } else {
+    // The next update's integrate and calcHash for particle o: its position
+    // is sortedPos[i] (the reorder gathered pos[o]), its velocity nv with
+    // w = 0 as collide leaves it.
+    integrateOne(pos, nv, dt, ri, P);
+    posOut[o] = make_float4(pos.x, pos.y, pos.z, p4.w);
+    newVel[o] = make_float4(nv.x, nv.y, nv.z, 0.0f);
+    // The next calcHash.  Its index[o] = o is not stored: this kernel still
+    // reads the index array, and the next sort generates identity values.
+    int3 gn = gridPos(pos.x, pos.y, pos.z, P);
+    hashOut[o] = gridHash(gn.x, gn.y, gn.z, P);
+  }
+}
+
+template <int kMode, bool kRadiusFromW, bool kCollider, bool kForceOut>
+static void launchCollideT(unsigned blocks, float4 *newVel, float3 *force,
+                           const float4 *sp, const float4 *sv,
+                           const unsigned *index, const unsigned *cs,
+                           const unsigned *ce, unsigned n, const KParams &kp,
+                           float4 *posOut, unsigned *hashOut, float dt) {
+  kCollide<kMode, kRadiusFromW, kCollider, kForceOut>
+      <<<blocks, 128, 0, curStream()>>>(newVel, force, sp, sv, index, cs, ce, n,
+                                         kp, posOut, hashOut, dt);
+}
+
+void launchCollide(int mode, bool collider, float4 *newVel, float3 *force,
+                   const float4 *sp, const float4 *sv, const unsigned *index,
+                   const unsigned *cs, const unsigned *ce, unsigned n,
+                   const KParams &kp, float4 *posOut, unsigned *hashOut,
+                   float dt) {
+  if (n == 0) return;
+  unsigned blocks = (n + 127) / 128;
+  bool w = kp.radiusFromW != 0;
+  bool fo = force != nullptr;
+#define FCDEM_COLLIDE_CASE(M, W, C, F)                                        \
+  if (mode == M && w == W && collider == C && fo == F) {                      \
+    launchCollideT<M, W, C, F>(blocks, newVel, force, sp, sv, index, cs, ce,  \
+                               n, kp, posOut, hashOut, dt);                    \
+    launchOk();                                                               \
+    return;                                                                   \
+  }
+  FCDEM_COLLIDE_CASE(0, false, true, false)
+  FCDEM_COLLIDE_CASE(0, true, true, false)
+  FCDEM_COLLIDE_CASE(0, false, false, false)
+  FCDEM_COLLIDE_CASE(0, true, false, false)
+  FCDEM_COLLIDE_CASE(0, false, false, true)
+  FCDEM_COLLIDE_CASE(0, true, false, true)
+  FCDEM_COLLIDE_CASE(0, false, true, true)
+  FCDEM_COLLIDE_CASE(0, true, true, true)
+  FCDEM_COLLIDE_CASE(1, false, true, false)
+  FCDEM_COLLIDE_CASE(1, true, true, false)
+#undef FCDEM_COLLIDE_CASE
+  setError(FCDEM_ERR_INVALID_VALUE);
+}
+
+void launchIntegrateHash(float4 *pos, float4 *vel, float dt, unsigned *hash,
+                         unsigned *index, unsigned n, const KParams &kp) {
+  if (n == 0) return;
+  kIntegrateHash<<<(n + 255) / 256, 256, 0, curStream()>>>(pos, vel, dt, hash,
+                                                           index, n, kp);
+  launchOk();
+}
+
+void launchReorder(unsigned *cellStart, unsigned *cellEnd, float4 *sortedPos,
+                   float4 *sortedVel, const unsigned *hash,
+                   const unsigned *index, const float4 *oldPos,
+                   const float4 *oldVel, unsigned n) {
+  if (n == 0) return;
+  kReorder<<<(n + 255) / 256, 256, 0, curStream()>>>(
+      cellStart, cellEnd, sortedPos, sortedVel, hash, index, oldPos, oldVel, n);
+  launchOk();
+}
+
+static bool gridOk(const SimParams &p) {
+  for (int k = 0; k < 3; ++k) {
+    unsigned g = p.gridSize[k];
+    if (g == 0 || (g & (g - 1)) != 0) return false;
+  }
+  return true;
+}
+
+bool readyFor(const Context &c) {
+  if (!c.haveParams) { setError(FCDEM_ERR_NO_PARAMS); return false; }
+  if (!gridOk(c.params)) { setError(FCDEM_ERR_INVALID_VALUE); return false; }
+  return true;
+}
+
+}  // namespace fcdem
+
+using namespace fcdem;
+
+extern "C" {
+
+void integrateSystem(float *pos, float *vel, float deltaTime, uint numParticles) {
+  Context &c = ctx();
+  if (!c.haveParams) { setError(FCDEM_ERR_NO_PARAMS); return; }
+  if (numParticles == 0) return;
+  if (!pos || !vel) { setError(FCDEM_ERR_INVALID_VALUE); return; }
+  kIntegrate<<<(numParticles + 255) / 256, 256, 0, curStream()>>>(
+      (float4 *)pos, (float4 *)vel, deltaTime, numParticles, kparams(c));
+  launchOk();
+}
+
+void calcHash(uint *gridParticleHash, uint *gridParticleIndex, float *pos,
+              int numParticles) {
+  Context &c = ctx();
+  if (!readyFor(c)) return;
+  if (numParticles <= 0) {
+    if (numParticles < 0) setError(FCDEM_ERR_INVALID_VALUE);
+    return;
+  }
+  if (!gridParticleHash || !gridParticleIndex || !pos) {
+    setError(FCDEM_ERR_INVALID_VALUE);
+    return;
+  }
+  unsigned n = (unsigned)numParticles;
+  kCalcHash<<<(n + 255) / 256, 256, 0, curStream()>>>(
+      gridParticleHash, gridParticleIndex, (const float4 *)pos, n, kparams(c));
+  launchOk();
+}
+
+void reorderDataAndFindCellStart(uint *cellStart, uint *cellEnd,
+                                 float *sortedPos, float *sortedVel,
+                                 uint *gridParticleHash, uint *gridParticleIndex,
+                                 float *oldPos, float *oldVel,
+                                 uint numParticles, uint numCells) {
+  Context &c = ctx();
+  if (!cellStart || (numParticles && (!cellEnd || !sortedPos || !sortedVel ||
+                                      !gridParticleHash || !gridParticleIndex ||
+                                      !oldPos || !oldVel))) {
+    setError(FCDEM_ERR_INVALID_VALUE);
+    return;
+  }
+  fillU32(c, cellStart, numCells, kEmpty);
+  launchReorder(cellStart, cellEnd, (float4 *)sortedPos, (float4 *)sortedVel,
+                gridParticleHash, gridParticleIndex, (const float4 *)oldPos,
+                (const float4 *)oldVel, numParticles);
+}
+
+void collide(float *newVel, float *sortedPos, float *sortedVel,
+             uint *gridParticleIndex, uint *cellStart, uint *cellEnd,
+             uint numParticles, uint numCells) {
+  (void)numCells;
+  Context &c = ctx();
+  if (!readyFor(c)) return;
+  if (numParticles == 0) return;
+  if (!newVel || !sortedPos || !sortedVel || !gridParticleIndex || !cellStart ||
+      !cellEnd) {
+    setError(FCDEM_ERR_INVALID_VALUE);
+    return;
+  }
+  launchCollide(0, true, (float4 *)newVel, nullptr, (const float4 *)sortedPos,
+                (const float4 *)sortedVel, gridParticleIndex, cellStart,
+                cellEnd, numParticles, kparams(c), nullptr, nullptr, 0.0f);
+}
+
+void sortParticles(uint *dGridParticleHash, uint *dGridParticleIndex,
+                   uint numParticles) {
+  Context &c = ctx();
+  if (numParticles < 2) return;
+  if (!dGridParticleHash || !dGridParticleIndex) {
+    setError(FCDEM_ERR_INVALID_VALUE);
+    return;
+  }
+  int bits = c.haveParams ? keyBits(c.params.numCells) : 32;
+  radixSortPairs(c, dGridParticleHash, dGridParticleIndex, numParticles, bits);
+}
+
+void fcdemUpdate(float *pos, float *vel, float *sortedPos, float *sortedVel,
+                 uint *hash, uint *index, uint *cellStart, uint *cellEnd,
+                 float deltaTime, uint numParticles, uint numCells, uint steps) {
+  Context &c = ctx();
+  if (!readyFor(c)) return;
+  if (steps == 0 || numParticles == 0) return;
+  if (!pos || !vel || !sortedPos || !sortedVel || !hash || !index ||
+      !cellStart || !cellEnd || numCells == 0) {
+    setError(FCDEM_ERR_INVALID_VALUE);
+    return;
+  }
+  const KParams kp = kparams(c);
+  const int bits = keyBits(c.params.numCells);
+  const unsigned n = numParticles;
+  stageBegin(0);
+  launchIntegrateHash((float4 *)pos, (float4 *)vel, deltaTime, hash, index, n, kp);
+  stageEnd(0);
+  for (uint s = 0; s < steps; ++s) {
+    // After the first step the fused collide has written the keys but not
+    // the identity index (see kCollide); the sort generates it.
+    stageBegin(1);
+    radixSortPairs(c, hash, index, n, bits, /*identityVals=*/s > 0);
+    stageEnd(1);
+    stageBegin(2);
+    fillU32(c, cellStart, numCells, kEmpty);
+    stageEnd(2);
+    stageBegin(3);
+    launchReorder(cellStart, cellEnd, (float4 *)sortedPos, (float4 *)sortedVel,
+                  hash, index, (const float4 *)pos, (const float4 *)vel, n);
+    stageEnd(3);
+    const bool last = (s + 1 == steps);
+    stageBegin(4);
+    launchCollide(last ? 0 : 1, true, (float4 *)vel, nullptr,
+                  (const float4 *)sortedPos, (const float4 *)sortedVel, index,
+                  cellStart, cellEnd, n, kp, (float4 *)pos, hash, deltaTime);
+    stageEnd(4);
+  }
+}
+
+}  // extern "C"

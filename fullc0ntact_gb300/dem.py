@@ -1,0 +1,205 @@
+"""Python face of libfcdem: the reference-named stages on torch device
+tensors, a device-resident scene, and the ParticleSystem wrapper.
+
+torch is used only to own device memory and streams; every computation is a
+call into libfcdem.so through its C-ABI.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _native
+from .params import SimParams
+
+lib = _native.lib
+check = _native.check
+
+
+def _p(t: torch.Tensor) -> int:
+    if not t.is_cuda:
+        raise ValueError("libfcdem stages take CUDA tensors")
+    if not t.is_contiguous():
+        raise ValueError("libfcdem stages take contiguous tensors")
+    return t.data_ptr()
+
+
+# --- the five stages, reference names and argument order -------------------
+
+def set_parameters(params: SimParams) -> None:
+    lib.setParameters(C.byref(params))
+
+
+def set_radius_mode(radius_from_w: bool) -> None:
+    lib.fcdemSetRadiusMode(1 if radius_from_w else 0)
+
+
+def set_stream(stream: torch.cuda.Stream | None) -> None:
+    lib.fcdemSetStream(None if stream is None else stream.cuda_stream)
+
+
+def integrate_system(pos, vel, dt: float, n: int) -> None:
+    lib.integrateSystem(_p(pos), _p(vel), dt, n)
+
+
+def calc_hash(hash_, index, pos, n: int) -> None:
+    lib.calcHash(_p(hash_), _p(index), _p(pos), n)
+
+
+def sort_particles(hash_, index, n: int) -> None:
+    lib.sortParticles(_p(hash_), _p(index), n)
+
+
+def reorder_data_and_find_cell_start(cell_start, cell_end, sorted_pos, sorted_vel,
+                                     hash_, index, old_pos, old_vel, n: int,
+                                     num_cells: int) -> None:
+    lib.reorderDataAndFindCellStart(_p(cell_start), _p(cell_end), _p(sorted_pos),
+                                    _p(sorted_vel), _p(hash_), _p(index), _p(old_pos),
+                                    _p(old_vel), n, num_cells)
+
+
+def collide(new_vel, sorted_pos, sorted_vel, index, cell_start, cell_end, n: int,
+            num_cells: int) -> None:
+    lib.collide(_p(new_vel), _p(sorted_pos), _p(sorted_vel), _p(index), _p(cell_start),
+                _p(cell_end), n, num_cells)
+
+
+lib.fcdemUpdate.argtypes = [C.c_void_p] * 8 + [C.c_float, C.c_uint, C.c_uint, C.c_uint]
+lib.fcdemUpdate.restype = None
+
+
+def update(pos, vel, sorted_pos, sorted_vel, hash_, index, cell_start, cell_end,
+           dt: float, n: int, num_cells: int, steps: int = 1) -> None:
+    lib.fcdemUpdate(_p(pos), _p(vel), _p(sorted_pos), _p(sorted_vel), _p(hash_),
+                    _p(index), _p(cell_start), _p(cell_end), dt, n, num_cells, steps)
+
+
+# --- device-resident scene -------------------------------------------------
+
+class DeviceScene:
+    """The work arrays of ParticleSystem (particleSystem.cpp:117-190) for one
+    scene, as torch CUDA tensors."""
+
+    def __init__(self, scene: dict, device: str | torch.device = "cuda"):
+        self.params: SimParams = scene["params"].copy()
+        self.radius_from_w = bool(scene.get("radius_from_w", False))
+        self.dt = float(scene.get("dt", 0.5))
+        self.n = int(scene["pos"].shape[0])
+        self.num_cells = int(self.params.numCells)
+        dev = torch.device(device)
+        self.pos = torch.from_numpy(np.ascontiguousarray(scene["pos"])).to(dev)
+        self.vel = torch.from_numpy(np.ascontiguousarray(scene["vel"])).to(dev)
+        self.sorted_pos = torch.empty_like(self.pos)
+        self.sorted_vel = torch.empty_like(self.vel)
+        self.hash = torch.empty(self.n, dtype=torch.int32, device=dev)
+        self.index = torch.empty(self.n, dtype=torch.int32, device=dev)
+        self.cell_start = torch.empty(self.num_cells, dtype=torch.int32, device=dev)
+        self.cell_end = torch.full((self.num_cells,), -1, dtype=torch.int32, device=dev)
+
+    def activate(self) -> None:
+        set_parameters(self.params)
+        set_radius_mode(self.radius_from_w)
+
+    def stages(self, dt: float | None = None) -> None:
+        """One update as the reference issues it: five separate calls."""
+        dt = self.dt if dt is None else dt
+        self.activate()
+        integrate_system(self.pos, self.vel, dt, self.n)
+        calc_hash(self.hash, self.index, self.pos, self.n)
+        sort_particles(self.hash, self.index, self.n)
+        reorder_data_and_find_cell_start(self.cell_start, self.cell_end, self.sorted_pos,
+                                         self.sorted_vel, self.hash, self.index, self.pos,
+                                         self.vel, self.n, self.num_cells)
+        collide(self.vel, self.sorted_pos, self.sorted_vel, self.index, self.cell_start,
+                self.cell_end, self.n, self.num_cells)
+
+    def update(self, steps: int = 1, dt: float | None = None) -> None:
+        """`steps` updates through the fused fcdemUpdate."""
+        dt = self.dt if dt is None else dt
+        self.activate()
+        update(self.pos, self.vel, self.sorted_pos, self.sorted_vel, self.hash,
+               self.index, self.cell_start, self.cell_end, dt, self.n, self.num_cells,
+               steps)
+
+
+def u32(t: torch.Tensor) -> np.ndarray:
+    """int32 device tensor -> uint32 host array (same bits)."""
+    return t.cpu().numpy().view(np.uint32)
+
+
+# --- ParticleSystem (C++ class behind a C wrapper) --------------------------
+
+_PS_SIGS = {
+    "fcdemPS_create": (C.c_void_p, [C.c_uint] * 4),
+    "fcdemPS_destroy": (None, [C.c_void_p]),
+    "fcdemPS_params": (C.POINTER(SimParams), [C.c_void_p]),
+    "fcdemPS_update": (None, [C.c_void_p, C.c_float]),
+    "fcdemPS_updateSteps": (None, [C.c_void_p, C.c_float, C.c_uint]),
+    "fcdemPS_reset": (None, [C.c_void_p, C.c_int]),
+    "fcdemPS_setArray": (None, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int]),
+    "fcdemPS_getArray": (C.POINTER(C.c_float), [C.c_void_p, C.c_int]),
+    "fcdemPS_dumpGrid": (C.c_uint, [C.c_void_p]),
+    "fcdemPS_setFusedUpdate": (None, [C.c_void_p, C.c_int]),
+    "fcdemPS_setRadiusFromW": (None, [C.c_void_p, C.c_int]),
+    "fcdemPS_devicePos": (C.c_void_p, [C.c_void_p]),
+    "fcdemPS_deviceVel": (C.c_void_p, [C.c_void_p]),
+}
+for _n, (_r, _a) in _PS_SIGS.items():
+    getattr(lib, _n).restype = _r
+    getattr(lib, _n).argtypes = _a
+
+
+class ParticleSystem:
+    """The reference's ParticleSystem (particleSystem.h:22-136), headless:
+    constructor(numParticles, gridSize), update(dt), reset(config),
+    getArray/setArray, the setters, dumpGrid."""
+
+    CONFIG_RANDOM, CONFIG_GRID = 0, 1
+    POSITION, VELOCITY = 0, 1
+
+    def __init__(self, num_particles: int, grid_size=(64, 64, 64)):
+        self.n = int(num_particles)
+        self._h = lib.fcdemPS_create(self.n, *[int(g) for g in grid_size])
+        if not self._h:
+            raise MemoryError("fcdemPS_create failed")
+        check("ParticleSystem()")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib.fcdemPS_destroy(h)
+            self._h = None
+
+    @property
+    def params(self) -> SimParams:
+        return lib.fcdemPS_params(self._h).contents
+
+    def update(self, dt: float) -> None:
+        lib.fcdemPS_update(self._h, dt)
+
+    def update_steps(self, dt: float, steps: int) -> None:
+        lib.fcdemPS_updateSteps(self._h, dt, steps)
+
+    def reset(self, config: int) -> None:
+        lib.fcdemPS_reset(self._h, config)
+
+    def set_array(self, array: int, data: np.ndarray, start: int = 0,
+                  count: int | None = None) -> None:
+        data = np.ascontiguousarray(data, np.float32)
+        count = data.shape[0] if count is None else count
+        lib.fcdemPS_setArray(self._h, array, data.ctypes.data, start, count)
+
+    def get_array(self, array: int) -> np.ndarray:
+        p = lib.fcdemPS_getArray(self._h, array)
+        return np.ctypeslib.as_array(p, shape=(self.n, 4)).copy()
+
+    def dump_grid(self) -> int:
+        return int(lib.fcdemPS_dumpGrid(self._h))
+
+    def set_fused_update(self, fused: bool) -> None:
+        lib.fcdemPS_setFusedUpdate(self._h, int(fused))
+
+    def set_radius_from_w(self, on: bool) -> None:
+        lib.fcdemPS_setRadiusFromW(self._h, int(on))

@@ -1,0 +1,102 @@
+"""Seeded synthetic scenes (host numpy arrays) for the particle-DEM step.
+
+Every scene is a dict with ``pos`` and ``vel`` ((n, 4) float32), ``params``
+(SimParams), ``radius_from_w`` (polydisperse mode) and ``dt``.  The reference
+ships no benchmark data: these generators restate its scene set-up
+(particleSystem.cpp:380-402, particledem_um.cu:233-326) and extend it to the
+polydisperse packed case.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _native
+from .params import SimParams, make_params
+
+_lib = _native.lib
+_f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+_lib.fcdemSceneLattice.argtypes = [_f32p, _f32p, C.c_uint, C.c_float, C.c_float,
+                                   C.c_float, C.c_float, C.c_ulonglong]
+_lib.fcdemSceneLattice.restype = None
+_lib.fcdemScenePack.argtypes = [_f32p, _f32p, C.c_uint, _f32p, _f32p, C.c_float,
+                                C.c_float, C.c_float, C.c_float, C.c_ulonglong, C.c_uint]
+_lib.fcdemScenePack.restype = C.c_uint
+
+
+def lattice(n: int, radius: float, jitter: float, vel_range: float, seed: int,
+            spacing: float | None = None):
+    pos = np.zeros((n, 4), np.float32)
+    vel = np.zeros((n, 4), np.float32)
+    sp = 2.0 * radius if spacing is None else spacing
+    _lib.fcdemSceneLattice(pos, vel, n, radius, sp, jitter, vel_range, seed)
+    return pos, vel
+
+
+def pack(n: int, box_min, box_max, r_median: float, sigma: float, r_max: float,
+         vel_range: float, seed: int, max_attempts: int = 20000):
+    pos = np.zeros((n, 4), np.float32)
+    vel = np.zeros((n, 4), np.float32)
+    placed = _lib.fcdemScenePack(pos, vel, n, np.asarray(box_min, np.float32),
+                                 np.asarray(box_max, np.float32), r_median, sigma,
+                                 r_max, vel_range, seed, max_attempts)
+    if placed != n:
+        raise RuntimeError(f"packing placed {placed} of {n} spheres")
+    return pos, vel
+
+
+def config0(n: int = 16384, seed: int = 1973) -> dict:
+    """Plain DEM: n monodisperse spheres of radius 1/64 on a jittered lattice
+    (spacing 2r, jitter 0.01r) in the [-1,1]^3 box, 64^3 grid with cell = 2r,
+    velocities U[-0.01, 0.01], gravity -3e-4, spring 0.5, damping 0.02,
+    shear 0.1, attraction 0, boundary damping -0.5, dt 0.5."""
+    r = 1.0 / 64.0
+    pos, vel = lattice(n, r, 0.01 * r, 0.01, seed)
+    return dict(name="plain-16k-64^3", pos=pos, vel=vel,
+                params=make_params(n, (64, 64, 64), r), radius_from_w=False, dt=0.5)
+
+
+def lognormal_mean_volume(r_median: float, sigma: float) -> float:
+    return 4.0 / 3.0 * math.pi * r_median ** 3 * math.exp(4.5 * sigma * sigma)
+
+
+def config1(n: int = 4194304, seed: int = 2024, grid: int = 256,
+            volume_fraction: float = 0.30) -> dict:
+    """Plain DEM at scale: n spheres with lognormal radii (median 1/512,
+    sigma 0.25, clipped at 2/512), cell = max diameter (grid cells span the
+    [-1,1] box), random sequential packing at the given volume fraction in a
+    centred cube, same contact parameters as config0.  Smaller n keep the
+    radii and the packing density (the cube shrinks)."""
+    r_med, sigma, r_max = 1.0 / 512.0, 0.25, 2.0 / 512.0
+    vol = n * lognormal_mean_volume(r_med, sigma)
+    side = (vol / volume_fraction) ** (1.0 / 3.0)
+    side = min(side, 2.0 - 4.0 * r_max)
+    lo = [-side / 2.0] * 3
+    hi = [side / 2.0] * 3
+    pos, vel = pack(n, lo, hi, r_med, sigma, r_max, 0.01, seed)
+    cell = 2.0 * r_max
+    g = grid
+    p = make_params(n, (g, g, g), particle_radius=r_max, cell_size=cell)
+    return dict(name=f"packed-{n}-{g}^3", pos=pos, vel=vel, params=p,
+                radius_from_w=True, dt=0.5, box_side=side)
+
+
+def random_box(n: int, grid=(16, 16, 16), radius: float = 1.0 / 16.0, seed: int = 7,
+               vel_range: float = 0.01, cell: float | None = None,
+               origin=(-1.0, -1.0, -1.0), poly: bool = False) -> dict:
+    """Uniform random positions in [-1,1]^3 (overlaps allowed), as
+    ParticleSystem::reset(CONFIG_RANDOM) places them."""
+    rng = np.random.default_rng(seed)
+    pos = np.zeros((n, 4), np.float32)
+    pos[:, :3] = rng.uniform(-1.0, 1.0, (n, 3)).astype(np.float32)
+    if poly:
+        pos[:, 3] = rng.uniform(0.5 * radius, radius, n).astype(np.float32)
+    else:
+        pos[:, 3] = 1.0
+    vel = np.zeros((n, 4), np.float32)
+    vel[:, :3] = rng.uniform(-vel_range, vel_range, (n, 3)).astype(np.float32)
+    p = make_params(n, grid, radius, cell_size=cell, world_origin=origin)
+    return dict(name=f"random-{n}", pos=pos, vel=vel, params=p, radius_from_w=poly,
+                dt=0.5)

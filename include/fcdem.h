@@ -1,0 +1,206 @@
+/*
+ * fcdem.h -- C-ABI of the GB300 (sm_103a) particle-DEM step.
+ *
+ * The first block of entry points has exactly the names, argument lists and
+ * meaning of FullC0ntact's particle-system C interface
+ * (cuda_addon/particleSystem.cuh:12-63, implemented in
+ * cuda_addon/particleSystem.cu:99-335), so host code written against that
+ * header links against libfcdem.so unchanged.  Pointers are DEVICE pointers;
+ * positions and velocities are float4 per particle (x, y, z, w), 16 bytes.
+ *
+ * Behaviour kept from the reference:
+ *   - every stage is issued in order on one CUDA stream (the legacy default
+ *     stream unless fcdemSetStream() names another one);
+ *   - calcHash writes index[i] = i; sortParticles is a stable ascending sort of
+ *     (hash, index) pairs; reorderDataAndFindCellStart sets cellStart of empty
+ *     cells to 0xffffffff and leaves cellEnd of empty cells untouched;
+ *   - collide writes newVel[index[i]] = (v + F, 0) where F is the summed
+ *     spring/dashpot/shear/attraction term over the 27 wrapped neighbour cells
+ *     plus the collider sphere term.
+ * Differences:
+ *   - no entry point calls exit(); failures are recorded and returned by
+ *     fcdemGetLastError();
+ *   - the OpenGL interop entry points exist only as stubs that record
+ *     FCDEM_ERR_UNSUPPORTED (no graphics stack on the target);
+ *   - extensions are prefixed fcdem* and documented below.
+ */
+#ifndef FCDEM_H
+#define FCDEM_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------------- */
+/* SimParams: 104 bytes, 4-byte aligned, field order and offsets of
+ * cuda_addon/particles_kernel.cuh:27-48.  When the reference header has been
+ * included first (its guard is PARTICLES_KERNEL_H) its definition is used. */
+#ifndef PARTICLES_KERNEL_H
+typedef unsigned int uint;
+typedef struct SimParams {
+  float colliderPos[3];        /*   0 */
+  float colliderRadius;        /*  12 */
+  float gravity[3];            /*  16 */
+  float globalDamping;         /*  28 */
+  float particleRadius;        /*  32 */
+  unsigned int gridSize[3];    /*  36  each a power of two */
+  unsigned int numCells;       /*  48 */
+  float worldOrigin[3];        /*  52 */
+  float cellSize[3];           /*  64 */
+  unsigned int numBodies;      /*  76 */
+  unsigned int maxParticlesPerCell; /* 80  unused, as in the reference */
+  float spring;                /*  84 */
+  float damping;               /*  88 */
+  float shear;                 /*  92 */
+  float attraction;            /*  96 */
+  float boundaryDamping;       /* 100 */
+} SimParams;
+#endif
+
+struct cudaGraphicsResource;
+
+/* ---------------------------------------------------------------------- */
+/* Support calls (particleSystem.cuh:14-26). */
+
+/* particleSystem.cu:102-116: selects a device.  "-device=N" in argv picks N,
+ * otherwise device 0 (the GB300 build targets one GPU per process). */
+void cudaInit(int argc, char **argv);
+/* particleSystem.cu:128-131 (the implementation takes size_t; the reference
+ * header says int). */
+void allocateArray(void **devPtr, size_t size);
+/* particleSystem.cu:133-136 */
+void freeArray(void *devPtr);
+/* particleSystem.cu:138-141: waits for all work issued by this library. */
+void threadSync(void);
+/* particleSystem.cu:174-184: a non-null GL resource records
+ * FCDEM_ERR_UNSUPPORTED and copies nothing. */
+void copyArrayFromDevice(void *host, const void *device,
+                         struct cudaGraphicsResource **cuda_vbo_resource,
+                         int size);
+/* particleSystem.cu:143-146 */
+void copyArrayToDevice(void *device, const void *host, int offset, int size);
+/* particleSystem.cu:148-172: OpenGL interop.  Stubs: record
+ * FCDEM_ERR_UNSUPPORTED; map returns NULL. */
+void registerGLBufferObject(uint vbo, struct cudaGraphicsResource **cuda_vbo_resource);
+void unregisterGLBufferObject(struct cudaGraphicsResource *cuda_vbo_resource);
+void *mapGLBufferObject(struct cudaGraphicsResource **cuda_vbo_resource);
+void unmapGLBufferObject(struct cudaGraphicsResource *cuda_vbo_resource);
+
+/* ---------------------------------------------------------------------- */
+/* The five stages (particleSystem.cuh:29-61). */
+
+/* particleSystem.cu:186-190: copies the parameter block; every later launch
+ * on this device uses this copy until the next call. */
+void setParameters(SimParams *hostParams);
+
+/* particleSystem.cu:204-216 + particles_kernel.cu:39-75:
+ * v += g*dt; v *= globalDamping; p += v*dt; clamp to [-1+r, 1-r] per axis
+ * with v_axis *= boundaryDamping on contact.  In place. */
+void integrateSystem(float *pos, float *vel, float deltaTime, uint numParticles);
+
+/* particleSystem.cu:228-244 + particles_kernel.cu:78-115:
+ * hash[i] = wrapped linear cell id of pos[i], index[i] = i. */
+void calcHash(uint *gridParticleHash, uint *gridParticleIndex, float *pos,
+              int numParticles);
+
+/* particleSystem.cu:328-333: stable ascending sort of (hash, index) in place.
+ * Keys are expected below 2^ceil(log2(numCells)) of the current parameters;
+ * a larger key records FCDEM_ERR_KEY_RANGE. */
+void sortParticles(uint *dGridParticleHash, uint *dGridParticleIndex,
+                   uint numParticles);
+
+/* particleSystem.cu:246-285 + particles_kernel.cu:119-182 */
+void reorderDataAndFindCellStart(uint *cellStart, uint *cellEnd,
+                                 float *sortedPos, float *sortedVel,
+                                 uint *gridParticleHash, uint *gridParticleIndex,
+                                 float *oldPos, float *oldVel,
+                                 uint numParticles, uint numCells);
+
+/* particleSystem.cu:287-325 + particles_kernel.cu:185-293 */
+void collide(float *newVel, float *sortedPos, float *sortedVel,
+             uint *gridParticleIndex, uint *cellStart, uint *cellEnd,
+             uint numParticles, uint numCells);
+
+/* ---------------------------------------------------------------------- */
+/* Extensions (no counterpart in particleSystem.cuh). */
+
+#define FCDEM_SUCCESS               0
+#define FCDEM_ERR_INVALID_VALUE     1  /* bad size, null pointer, bad grid   */
+#define FCDEM_ERR_CUDA              2  /* a CUDA runtime call failed          */
+#define FCDEM_ERR_NO_PARAMS         3  /* a stage ran before setParameters   */
+#define FCDEM_ERR_UNSUPPORTED       4  /* OpenGL interop                      */
+#define FCDEM_ERR_DEVICE_TIMEOUT    5  /* a bounded device-side wait expired  */
+#define FCDEM_ERR_KEY_RANGE         6  /* sort key above the grid's key width */
+#define FCDEM_ERR_ALLOC             7  /* device scratch allocation failed    */
+
+/* Returns and clears the first error recorded since the last call.  It
+ * synchronises the library stream so that device-side status words (bounded
+ * waits, key-range checks) are included. */
+int fcdemGetLastError(void);
+const char *fcdemGetErrorString(int code);
+
+/* All later calls on this host thread's device issue their work on `stream`
+ * (a cudaStream_t; NULL = legacy default stream). */
+void fcdemSetStream(void *stream);
+
+/* 0 (default): every particle has radius SimParams.particleRadius, exactly as
+ * the reference.  1: the radius of particle i is pos[i].w (polydisperse
+ * scenes); collide uses radiusA = r_i, radiusB = r_j, which
+ * collideSpheres(particles_kernel.cu:185-218) accepts but collideCell never
+ * passes, and integrate clamps with r_i. */
+void fcdemSetRadiusMode(int radiusFromW);
+
+/* Library version string. */
+const char *fcdemVersion(void);
+
+/* `steps` consecutive ParticleSystem::update calls
+ * (particleSystem.cpp:222-284) in one call.  The stages are fused: the first
+ * integrate with its calcHash, and every collide except the last with the
+ * next update's integrate and calcHash.  On return pos, vel and every work
+ * array hold what `steps` reference updates leave in them (cellEnd of empty
+ * cells aside, which the reference leaves stale too). */
+void fcdemUpdate(float *pos, float *vel, float *sortedPos, float *sortedVel,
+                 uint *gridParticleHash, uint *gridParticleIndex,
+                 uint *cellStart, uint *cellEnd, float deltaTime,
+                 uint numParticles, uint numCells, uint steps);
+
+/* Number of kernels this library has launched in this process. */
+unsigned long long fcdemGetLaunchCount(void);
+
+/* Stage timing of fcdemUpdate.  With profiling on, fcdemUpdate records a CUDA
+ * event pair around each stage on its stream.  fcdemGetStageTimes
+ * synchronises, adds the elapsed times of the recorded pairs to per-stage
+ * totals, writes min(maxStages, FCDEM_NUM_STAGES) totals in milliseconds and
+ * the number of timed launches of each stage, and returns FCDEM_NUM_STAGES.
+ * Stages: 0 integrate+hash, 1 sort, 2 cell-table fill, 3 reorder,
+ * 4 collide.  fcdemSetProfiling(0/1) also clears the totals. */
+#define FCDEM_NUM_STAGES 5
+void fcdemSetProfiling(int on);
+int fcdemGetStageTimes(float *ms, unsigned *launches, int maxStages);
+
+/* ---------------------------------------------------------------------- */
+/* Scene generators (host memory, 4 floats per particle).  Deterministic for
+ * a given seed on every platform. */
+
+/* Jittered lattice of ParticleSystem::initGrid (particleSystem.cpp:380-402):
+ * side s = ceil(n^(1/3)) particles, pos = spacing*(x,y,z) + radius - 1 +
+ * U(-jitter, jitter), w = 1; velocities U(-velRange, velRange), w = 0. */
+void fcdemSceneLattice(float *pos4, float *vel4, uint n, float radius,
+                       float spacing, float jitter, float velRange,
+                       unsigned long long seed);
+
+/* Random sequential packing of n spheres with lognormal radii (median rMedian,
+ * log-sigma sigma, clipped to rMax) inside [boxMin, boxMax]; pos.w = radius.
+ * Radii are placed largest first; a sphere that finds no free spot after
+ * maxAttempts tries ends the packing.  Returns the number placed. */
+uint fcdemScenePack(float *pos4, float *vel4, uint n, const float boxMin[3],
+                    const float boxMax[3], float rMedian, float sigma, float rMax,
+                    float velRange, unsigned long long seed, uint maxAttempts);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FCDEM_H */

@@ -1,0 +1,114 @@
+"""Whole updates: the fused fcdemUpdate leaves the same state as the five
+reference-named calls; the C++ ParticleSystem drives them; multi-step runs
+agree with the oracle in energy, momentum and contact statistics."""
+import numpy as np
+import pytest
+import torch
+
+from fcdem_testutil import oracle_params
+
+pytestmark = pytest.mark.gpu
+
+
+def _state(ds):
+    return (ds.pos.cpu().numpy().copy(), ds.vel.cpu().numpy().copy(),
+            ds.hash.cpu().numpy().copy(), ds.index.cpu().numpy().copy(),
+            ds.sorted_pos.cpu().numpy().copy(), ds.sorted_vel.cpu().numpy().copy())
+
+
+@pytest.mark.parametrize("poly", [False, True])
+@pytest.mark.parametrize("steps", [1, 2, 5])
+def test_fused_update_equals_staged(poly, steps):
+    from fullc0ntact_gb300 import dem, scenes
+    sc = (scenes.random_box(5000, grid=(32, 32, 32), radius=1.0 / 24.0, seed=3, poly=True)
+          if poly else scenes.config0(4096))
+    a, b = dem.DeviceScene(sc), dem.DeviceScene(sc)
+    for _ in range(steps):
+        a.stages()
+    b.update(steps)
+    dem.check("update")
+    for x, y in zip(_state(a), _state(b)):
+        np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
+    cs_a, cs_b = a.cell_start.cpu().numpy(), b.cell_start.cpu().numpy()
+    np.testing.assert_array_equal(cs_a, cs_b)
+    ne = cs_a != -1
+    np.testing.assert_array_equal(a.cell_end.cpu().numpy()[ne], b.cell_end.cpu().numpy()[ne])
+
+
+def test_particle_system_class():
+    """The headless ParticleSystem with the reference's defaults."""
+    from fullc0ntact_gb300 import dem
+    ps = dem.ParticleSystem(4096, (64, 64, 64))
+    p = ps.params
+    assert abs(p.particleRadius - 1.0 / 16.0) < 1e-9 and p.numCells == 64 ** 3
+    p.particleRadius = 1.0 / 64.0
+    p.cellSize[:] = [1.0 / 32.0] * 3
+    ps.reset(dem.ParticleSystem.CONFIG_GRID)
+    pos0 = ps.get_array(dem.ParticleSystem.POSITION)
+    assert np.all(pos0[:, 3] == 1.0) and pos0[:, :3].min() > -1.0
+    ps.set_fused_update(False)
+    ps.update(0.5)
+    ps.update(0.5)
+    staged = ps.get_array(dem.ParticleSystem.VELOCITY)
+    ps2 = dem.ParticleSystem(4096, (64, 64, 64))
+    ps2.params.particleRadius = 1.0 / 64.0
+    ps2.params.cellSize[:] = [1.0 / 32.0] * 3
+    ps2.reset(dem.ParticleSystem.CONFIG_GRID)
+    ps2.update_steps(0.5, 2)
+    fused = ps2.get_array(dem.ParticleSystem.VELOCITY)
+    np.testing.assert_array_equal(staged, fused)
+    assert ps2.dump_grid() >= 1
+    dem.check("ParticleSystem")
+
+
+def _stats(pos, vel, radius, gz=-3e-4):
+    v = vel[:, :3].astype(np.float64)
+    ke = 0.5 * np.sum(v * v)
+    pe = -gz * np.sum(pos[:, 2].astype(np.float64) + 1.0)
+    mom = v.sum(axis=0)
+    return ke, pe, mom
+
+
+def test_multistep_statistics_match_oracle():
+    """Trajectories are chaotic, so 50 steps are compared by total energy,
+    momentum and contact count, not particle by particle."""
+    from fullc0ntact_gb300 import dem, scenes
+    from oracle import oracle as O
+    sc = scenes.config0(8192)
+    ds = dem.DeviceScene(sc)
+    ds.update(50)
+    dem.check()
+    P = oracle_params(bytes(sc["params"]))
+    pos, vel = sc["pos"].copy(), sc["vel"].copy()
+    O.update(P, pos, vel, sc["dt"], steps=50)
+    g_pos, g_vel = ds.pos.cpu().numpy(), ds.vel.cpu().numpy()
+    ke_g, pe_g, mom_g = _stats(g_pos, g_vel, P.particleRadius)
+    ke_o, pe_o, mom_o = _stats(pos, vel, P.particleRadius)
+    assert abs(ke_g - ke_o) <= 0.02 * ke_o + 1e-12
+    assert abs(pe_g - pe_o) <= 1e-3 * abs(pe_o)
+    assert np.all(np.abs(mom_g - mom_o) <= 0.05 * np.abs(mom_o).max() + 1e-9)
+    # contact count of the final configuration
+    def contacts(p):
+        h, x = O.calc_hash(P, p)
+        hs, xs = O.sort_pairs(h, x)
+        cs, ce, sp, sv = O.reorder(hs, xs, p, vel, P.numCells)
+        nv = O.collide(P, sp, sv, xs, cs, ce)
+        return int(np.count_nonzero(np.any(nv[:, :3] != vel[:, :3], axis=1)))
+    c_g, c_o = contacts(g_pos), contacts(pos)
+    assert abs(c_g - c_o) <= 0.02 * c_o
+
+
+def test_stream_selection():
+    from fullc0ntact_gb300 import dem, scenes
+    sc = scenes.config0(2048)
+    a, b = dem.DeviceScene(sc), dem.DeviceScene(sc)
+    a.update(3)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        dem.set_stream(s)
+        b.update(3)
+        dem.set_stream(None)
+    s.synchronize()
+    dem.check()
+    np.testing.assert_array_equal(a.vel.cpu().numpy(), b.vel.cpu().numpy())
