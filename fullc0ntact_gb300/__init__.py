@@ -2,9 +2,10 @@
 FullC0ntact behind the reference's particleSystem C-ABI.
 
 The compute path is libfcdem.so (hand-written CUDA, built in-tree by
-``fullc0ntact_gb300.build``); importing the package without it raises.
+``fullc0ntact_gb300.build``).  The modules that call it (``dem``, ``scenes``)
+load it through ``_native``, which raises ImportError when it is missing:
+there is no CPU fallback.
 """
 from .params import SimParams, make_params  # noqa: F401
-from . import _native  # noqa: F401  (raises ImportError without libfcdem.so)
 
 __all__ = ["SimParams", "make_params"]

@@ -236,8 +236,10 @@ kOnesweep(const unsigned *__restrict__ keysIn, const unsigned *__restrict__ vals
       unsigned k = sKeys[lp];
       unsigned d = (k >> shift) & (kRadix - 1);
       unsigned g = (unsigned)(sBase[d] + (int)lp);
-      keysOut[g] = k;
-      valsOut[g] = sVals[lp];
+      if (g < n) {  // always true unless a look-back wait timed out
+        keysOut[g] = k;
+        valsOut[g] = sVals[lp];
+      }
     }
   }
 }

@@ -92,21 +92,27 @@ kReorder(unsigned *__restrict__ cellStart, unsigned *__restrict__ cellEnd,
          float4 *__restrict__ sortedPos, float4 *__restrict__ sortedVel,
          const unsigned *__restrict__ hash, const unsigned *__restrict__ index,
          const float4 *__restrict__ oldPos, const float4 *__restrict__ oldVel,
-         unsigned n) {
+         unsigned n, unsigned numCells, unsigned *status) {
   unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   unsigned h = __ldg(hash + i);
+  unsigned s = __ldg(index + i);
+  // Hashes come from calcHash and are below numCells, indices below n; a
+  // caller's array that breaks this is reported instead of written through.
+  if (h >= numCells || s >= n) {
+    atomicOr(status, (unsigned)kStatusKeyRange);
+    return;
+  }
   if (i == 0) {
     cellStart[h] = 0;
   } else {
     unsigned hp = __ldg(hash + i - 1);
     if (h != hp) {
       cellStart[h] = i;
-      cellEnd[hp] = i;
+      if (hp < numCells) cellEnd[hp] = i;
     }
   }
   if (i == n - 1) cellEnd[h] = n;
-  unsigned s = __ldg(index + i);
   sortedPos[i] = ldg4(oldPos + s);
   sortedVel[i] = ldg4(oldVel + s);
 }
@@ -152,7 +158,7 @@ kCollide(float4 *__restrict__ newVel, float3 *__restrict__ forceOut,
         unsigned start = __ldg(cellStart + h);
         float3 cf = make_float3(0.0f, 0.0f, 0.0f);
         if (start != kEmpty) {
-          unsigned end = __ldg(cellEnd + h);
+          unsigned end = min(__ldg(cellEnd + h), n);
           for (unsigned j = start; j < end; j++) {
             if (j == i) continue;
             float4 q4 = ldg4(sortedPos + j);
@@ -190,6 +196,7 @@ kCollide(float4 *__restrict__ newVel, float3 *__restrict__ forceOut,
     }
   }
   unsigned o = __ldg(index + i);
+  if (o >= n) return;  // not a permutation of 0..n-1: nothing to write to
   float3 nv = make_float3(vel.x + force.x, vel.y + force.y, vel.z + force.z);
   if (kForceOut) forceOut[o] = force;
   if (kMode == 0) {
@@ -260,18 +267,29 @@ void launchIntegrateHash(float4 *pos, float4 *vel, float dt, unsigned *hash,
 void launchReorder(unsigned *cellStart, unsigned *cellEnd, float4 *sortedPos,
                    float4 *sortedVel, const unsigned *hash,
                    const unsigned *index, const float4 *oldPos,
-                   const float4 *oldVel, unsigned n) {
+                   const float4 *oldVel, unsigned n, unsigned numCells) {
   if (n == 0) return;
   kReorder<<<(n + 255) / 256, 256, 0, curStream()>>>(
-      cellStart, cellEnd, sortedPos, sortedVel, hash, index, oldPos, oldVel, n);
+      cellStart, cellEnd, sortedPos, sortedVel, hash, index, oldPos, oldVel, n,
+      numCells, ctx().dStatus);
   launchOk();
 }
 
 static bool gridOk(const SimParams &p) {
+  unsigned long long cells = 1;
   for (int k = 0; k < 3; ++k) {
     unsigned g = p.gridSize[k];
     if (g == 0 || (g & (g - 1)) != 0) return false;
+    cells *= g;
   }
+  return cells <= p.numCells;  // every hash indexes the cell tables
+}
+
+// The cell tables the caller passes must cover every hash of the grid.
+static bool tablesOk(const SimParams &p, unsigned numCells) {
+  unsigned long long cells =
+      (unsigned long long)p.gridSize[0] * p.gridSize[1] * p.gridSize[2];
+  if (cells > numCells) { setError(FCDEM_ERR_INVALID_VALUE); return false; }
   return true;
 }
 
@@ -330,15 +348,14 @@ void reorderDataAndFindCellStart(uint *cellStart, uint *cellEnd,
   fillU32(c, cellStart, numCells, kEmpty);
   launchReorder(cellStart, cellEnd, (float4 *)sortedPos, (float4 *)sortedVel,
                 gridParticleHash, gridParticleIndex, (const float4 *)oldPos,
-                (const float4 *)oldVel, numParticles);
+                (const float4 *)oldVel, numParticles, numCells);
 }
 
 void collide(float *newVel, float *sortedPos, float *sortedVel,
              uint *gridParticleIndex, uint *cellStart, uint *cellEnd,
              uint numParticles, uint numCells) {
-  (void)numCells;
   Context &c = ctx();
-  if (!readyFor(c)) return;
+  if (!readyFor(c) || !tablesOk(c.params, numCells)) return;
   if (numParticles == 0) return;
   if (!newVel || !sortedPos || !sortedVel || !gridParticleIndex || !cellStart ||
       !cellEnd) {
@@ -366,7 +383,7 @@ void fcdemUpdate(float *pos, float *vel, float *sortedPos, float *sortedVel,
                  uint *hash, uint *index, uint *cellStart, uint *cellEnd,
                  float deltaTime, uint numParticles, uint numCells, uint steps) {
   Context &c = ctx();
-  if (!readyFor(c)) return;
+  if (!readyFor(c) || !tablesOk(c.params, numCells)) return;
   if (steps == 0 || numParticles == 0) return;
   if (!pos || !vel || !sortedPos || !sortedVel || !hash || !index ||
       !cellStart || !cellEnd || numCells == 0) {
@@ -390,7 +407,7 @@ void fcdemUpdate(float *pos, float *vel, float *sortedPos, float *sortedVel,
     stageEnd(2);
     stageBegin(3);
     launchReorder(cellStart, cellEnd, (float4 *)sortedPos, (float4 *)sortedVel,
-                  hash, index, (const float4 *)pos, (const float4 *)vel, n);
+                  hash, index, (const float4 *)pos, (const float4 *)vel, n, numCells);
     stageEnd(3);
     const bool last = (s + 1 == steps);
     stageBegin(4);

@@ -3,7 +3,8 @@ kernel code (tests/golden/gen_golden.py): every stage bit for bit."""
 import numpy as np
 import pytest
 
-from fcdem_testutil import GOLDEN_CASES, full_cells, load_golden, oracle_params
+from fcdem_testutil import (GOLDEN_CASES, assert_same_floats, full_cells, load_golden,
+                            oracle_params)
 from oracle import oracle as O
 
 
@@ -22,7 +23,7 @@ def test_oracle_matches_reference_fixture(name):
     np.testing.assert_array_equal(st["cellStart"], cs)
     np.testing.assert_array_equal(st["cellEnd"][g["cells"]], g["cell_end"])
     np.testing.assert_array_equal(st["sortedPos"], g["pos"][g["index_sorted"]])
-    np.testing.assert_array_equal(st["newVel"].view(np.uint32), g["new_vel"].view(np.uint32))
+    assert_same_floats(st["newVel"], g["new_vel"])
 
 
 def test_fixture_invariants():
