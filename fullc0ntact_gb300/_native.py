@@ -49,6 +49,8 @@ _SIGS = {
     "fcdemSetStream": (None, [vp]),
     "fcdemSetRadiusMode": (None, [C.c_int]),
     "fcdemVersion": (C.c_char_p, []),
+    "fcdemSetCollidePath": (None, [C.c_int]),
+    "fcdemSetCellCulling": (None, [C.c_int]),
 }
 
 for _name, (_res, _args) in _SIGS.items():

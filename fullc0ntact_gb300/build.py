@@ -19,6 +19,7 @@ SOURCES = [
     "fcdem_context.cu",
     "fcdem_stages.cu",
     "fcdem_sort.cu",
+    "fcdem_collide.cu",
     "fcdem_host.cpp",
 ]
 

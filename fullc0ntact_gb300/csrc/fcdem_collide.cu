@@ -1,0 +1,558 @@
+// fcdem_collide.cu -- the collide stage (particles_kernel.cu:185-293):
+// spring / dashpot / shear / attraction over the 27 wrapped neighbour cells
+// plus the collider sphere, written as newVel[index[i]] = (v + F, 0).
+//
+// Arithmetic order.  The reference sums each neighbour cell's pair terms into
+// a cell subtotal (collideCell) and adds the subtotals in z, y, x order
+// (collideD); within a cell the partners come in ascending sorted index.
+// Both kernels below keep exactly that order, so the float sums are the
+// reference's.
+//
+// Two kernels:
+//  * kCollideGlobal -- one thread per sorted particle, neighbours read
+//    through the read-only cache.  Used for scenes that do not suit tiling.
+//  * kCollideTiled  -- a CTA takes 128 consecutive sorted particles, splits
+//    them into row groups (same (y, z) grid row), and for each group stages
+//    in shared memory the 9 neighbour-row windows of the cell tables and the
+//    positions of every particle in them: the positions of a window are one
+//    contiguous run of the sorted array, copied by the bulk-copy engine
+//    (cp.async.bulk, completion on an mbarrier).  The pair loops then read
+//    shared memory only.  A group whose window wraps around the grid or does
+//    not fit falls back to the global-read loop.
+#include "fcdem_dem.cuh"
+
+namespace fcdem {
+namespace {
+
+constexpr unsigned kEmpty = 0xffffffffu;
+constexpr int kTileThreads = 128;
+constexpr int kWinMax = 128;      // cells per staged row window
+constexpr int kStageMax = 1536;   // staged positions (24 KB)
+constexpr int kMaxGroups = 4;     // staged row groups per tile
+constexpr unsigned kWaitLimit = 1u << 22;
+
+// ---------------------------------------------------------------------------
+// The per-particle pair loop over one neighbour cell, shared by both kernels.
+// `pos(j)` returns the position of sorted particle j (global or staged).
+template <bool kRadiusFromW, class PosFn>
+__device__ __forceinline__ void cellTerms(unsigned start, unsigned end, unsigned i,
+                                         float3 pos, float3 vel, float ri,
+                                         float cdMono, float cdMonoHi2,
+                                         const float4 *__restrict__ sortedVel,
+                                         const SimParams &P, PosFn posOf,
+                                         float3 &force) {
+  float3 cf = make_float3(0.0f, 0.0f, 0.0f);
+  for (unsigned j = start; j < end; j++) {
+    float4 q4 = posOf(j);
+    float3 rel = make_float3(q4.x - pos.x, q4.y - pos.y, q4.z - pos.z);
+    float d2 = pairDist2(rel);
+    float cd = kRadiusFromW ? ri + q4.w : cdMono;
+    float hi2 = kRadiusFromW ? rejectBound(cd) : cdMonoHi2;
+    if (d2 < hi2 && j != i) {
+      float dist = sqrtf(d2);
+      if (dist < cd) {
+        float4 w4 = ldg4(sortedVel + j);
+        float3 f = contactTerm(rel, dist, cd, vel, make_float3(w4.x, w4.y, w4.z),
+                               P.attraction, P);
+        cf.x = cf.x + f.x;
+        cf.y = cf.y + f.y;
+        cf.z = cf.z + f.z;
+      }
+    }
+  }
+  force.x = force.x + cf.x;
+  force.y = force.y + cf.y;
+  force.z = force.z + cf.z;
+}
+
+// Collider sphere (particles_kernel.cu:288) and the outputs of particle i.
+template <int kMode, bool kCollider, bool kForceOut>
+__device__ __forceinline__ void finishParticle(
+    unsigned i, unsigned n, float3 pos, float3 vel, float4 p4, float ri,
+    float3 force, const unsigned *__restrict__ index, float4 *__restrict__ newVel,
+    float3 *__restrict__ forceOut, float4 *__restrict__ posOut,
+    unsigned *__restrict__ hashOut, float dt, const SimParams &P) {
+  if (kCollider) {
+    float3 rel = make_float3(P.colliderPos[0] - pos.x, P.colliderPos[1] - pos.y,
+                             P.colliderPos[2] - pos.z);
+    float dist = pairDist(rel);
+    float cd = ri + P.colliderRadius;
+    if (dist < cd) {
+      float3 f = contactTerm(rel, dist, cd, vel, make_float3(0.0f, 0.0f, 0.0f), 0.0f, P);
+      force.x = force.x + f.x;
+      force.y = force.y + f.y;
+      force.z = force.z + f.z;
+    }
+  }
+  unsigned o = __ldg(index + i);
+  if (o >= n) return;  // not a permutation of 0..n-1: nothing to write to
+  float3 nv = make_float3(vel.x + force.x, vel.y + force.y, vel.z + force.z);
+  if (kForceOut) forceOut[o] = force;
+  if (kMode == 0) {
+    newVel[o] = make_float4(nv.x, nv.y, nv.z, 0.0f);
+  } else {
+    // The next update's integrate and calcHash for particle o: its position
+    // is sortedPos[i] (the reorder gathered pos[o]) and its velocity nv with
+    // w = 0 as collide leaves it.  index[o] = o is not stored (this kernel
+    // still reads the index array); the next sort generates identity values.
+    integrateOne(pos, nv, dt, ri, P);
+    posOut[o] = make_float4(pos.x, pos.y, pos.z, p4.w);
+    newVel[o] = make_float4(nv.x, nv.y, nv.z, 0.0f);
+    int3 gn = gridPos(pos.x, pos.y, pos.z, P);
+    hashOut[o] = gridHash(gn.x, gn.y, gn.z, P);
+  }
+}
+
+// Cell culling.  A neighbour cell whose box lies farther than the largest
+// possible contact distance R from the particle cannot hold a partner in
+// contact, so its pair terms are all +0.0 and skipping it leaves the sums
+// unchanged.  `CellCull` holds the squared distances from the particle to
+// the faces of its own cell; a neighbour at offset (dx, dy, dz) is at box
+// distance^2 = fx[dx] + fy[dy] + fz[dz].  Exactness needs (checked on the
+// host, culling is off otherwise): every grid dimension >= 3, so the 27
+// offsets hash to 27 different cells, and R <= the smallest cell size, so a
+// particle aliased into a neighbour hash by the wrap is farther than R.  The
+// bound carries a relative margin of 1e-4 and an absolute margin for the
+// float rounding of the face positions and of the cell assignment.
+struct CellCull {
+  float xl, xh, yl, yh, zl, zh;  // squared distances to the lower/upper faces
+  float r2;
+  // squared box distance contributed by offset d in {-1, 0, 1} of one axis
+  __device__ __forceinline__ static float pick(int d, float lo, float hi) {
+    return d < 0 ? lo : (d > 0 ? hi : 0.0f);
+  }
+};
+
+__device__ __forceinline__ CellCull makeCull(float3 p, int3 g, float R, const SimParams &P) {
+  const float px[3] = {p.x, p.y, p.z};
+  const int gi[3] = {g.x, g.y, g.z};
+  float mag = 1.0f;
+  float fl[3], fh[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float lo = P.worldOrigin[k] + (float)gi[k] * P.cellSize[k];
+    float hi = lo + P.cellSize[k];
+    float dl = fmaxf(px[k] - lo, 0.0f), dh = fmaxf(hi - px[k], 0.0f);
+    fl[k] = dl * dl;
+    fh[k] = dh * dh;
+    mag += fabsf(px[k]) + fabsf(lo) + fabsf(hi);
+  }
+  CellCull c;
+  c.xl = fl[0]; c.xh = fh[0];
+  c.yl = fl[1]; c.yh = fh[1];
+  c.zl = fl[2]; c.zh = fh[2];
+  const float Rs = R * 1.0001f + 1e-6f * mag;
+  c.r2 = Rs * Rs;
+  return c;
+}
+
+// Per-thread queue of near partners (shared memory, entry q of thread t at
+// [q * kQueueStride + t]).
+constexpr int kQueueLen = 16;
+constexpr int kQueueStride = 128;
+
+// The 27-cell loop with cell tables and positions read from global memory,
+// in two phases.  The scan over candidates only tests the squared distance
+// (see rejectBound) and queues the partners that may be in contact, with the
+// index of their neighbour cell; the queue is drained in order, where the
+// exact `dist < cd` test and the contact term run.  Contacts are thus
+// computed back to back instead of diverging inside the scan.  Sums: `cf`
+// gathers the terms of the current cell and is added to `force` when a
+// contact of a later cell arrives.  Cells without contacts would add +0.0,
+// which leaves a sum that started at +0.0 unchanged, so the result is the
+// reference's cell-by-cell sum.
+template <bool kRadiusFromW>
+__device__ __forceinline__ float3 neighbourForceGlobal(
+    unsigned i, unsigned n, float3 pos, float3 vel, float ri, int3 g, bool cull,
+    const float4 *__restrict__ sortedPos, const float4 *__restrict__ sortedVel,
+    const unsigned *__restrict__ cellStart, const unsigned *__restrict__ cellEnd,
+    const SimParams &P, unsigned *qj, unsigned char *qc) {
+  const float cdMono = ri + P.particleRadius;
+  const float cdMonoHi2 = rejectBound(cdMono);
+  // largest contact distance: r_i + particleRadius (in the radius-from-w
+  // mode particleRadius bounds every radius)
+  const CellCull cc = makeCull(pos, g, ri + P.particleRadius, P);
+  const float cullR2 = cull ? cc.r2 : __int_as_float(0x7f800000);  // +inf: no culling
+  float3 force = make_float3(0.0f, 0.0f, 0.0f);
+  float3 cf = make_float3(0.0f, 0.0f, 0.0f);
+  int cfCell = -1;
+  int qn = 0;
+  auto drain = [&]() {
+    for (int q = 0; q < qn; ++q) {
+      const unsigned j = qj[q * kQueueStride];
+      const int cell = qc[q * kQueueStride];
+      float4 q4 = ldg4(sortedPos + j);
+      float3 rel = make_float3(q4.x - pos.x, q4.y - pos.y, q4.z - pos.z);
+      float dist = sqrtf(pairDist2(rel));
+      float cd = kRadiusFromW ? ri + q4.w : cdMono;
+      if (dist < cd) {
+        if (cell != cfCell) {
+          force.x = force.x + cf.x;
+          force.y = force.y + cf.y;
+          force.z = force.z + cf.z;
+          cf = make_float3(0.0f, 0.0f, 0.0f);
+          cfCell = cell;
+        }
+        float4 w4 = ldg4(sortedVel + j);
+        float3 f = contactTerm(rel, dist, cd, vel, make_float3(w4.x, w4.y, w4.z),
+                               P.attraction, P);
+        cf.x = cf.x + f.x;
+        cf.y = cf.y + f.y;
+        cf.z = cf.z + f.z;
+      }
+    }
+    qn = 0;
+  };
+#pragma unroll 1
+  for (int row = 0; row < 9; row++) {
+    const int z = row / 3 - 1, y = row % 3 - 1;
+    const float rowD2 = CellCull::pick(z, cc.zl, cc.zh) + CellCull::pick(y, cc.yl, cc.yh);
+    if (rowD2 > cullR2) continue;
+    unsigned h[3], start[3], end[3];
+#pragma unroll
+    for (int x = 0; x < 3; x++) {
+      start[x] = kEmpty;
+      if (rowD2 + CellCull::pick(x - 1, cc.xl, cc.xh) <= cullR2) {
+        h[x] = gridHash(g.x + x - 1, g.y + y, g.z + z, P);
+        start[x] = __ldg(cellStart + h[x]);
+      }
+    }
+#pragma unroll
+    for (int x = 0; x < 3; x++)
+      end[x] = start[x] != kEmpty ? min(__ldg(cellEnd + h[x]), n) : 0u;
+#pragma unroll
+    for (int x = 0; x < 3; x++) {
+      const unsigned b = end[x];
+      for (unsigned j = start[x] != kEmpty ? start[x] : 0u; j < b; j++) {
+        float4 q4 = ldg4(sortedPos + j);
+        float3 rel = make_float3(q4.x - pos.x, q4.y - pos.y, q4.z - pos.z);
+        float d2 = pairDist2(rel);
+        float hi2 = kRadiusFromW ? rejectBound(ri + q4.w) : cdMonoHi2;
+        if (d2 < hi2 && j != i) {
+          if (qn == kQueueLen) drain();
+          qj[qn * kQueueStride] = j;
+          qc[qn * kQueueStride] = (unsigned char)(row * 3 + x);
+          ++qn;
+        }
+      }
+    }
+  }
+  drain();
+  force.x = force.x + cf.x;
+  force.y = force.y + cf.y;
+  force.z = force.z + cf.z;
+  return force;
+}
+
+template <int kMode, bool kRadiusFromW, bool kCollider, bool kForceOut>
+__global__ void __launch_bounds__(128)
+kCollideGlobal(float4 *__restrict__ newVel, float3 *__restrict__ forceOut,
+               const float4 *__restrict__ sortedPos, const float4 *__restrict__ sortedVel,
+               const unsigned *__restrict__ index, const unsigned *__restrict__ cellStart,
+               const unsigned *__restrict__ cellEnd, unsigned n, KParams kp,
+               float4 *__restrict__ posOut, unsigned *__restrict__ hashOut, float dt,
+               bool cull, unsigned *status) {
+  __shared__ unsigned qj[kQueueLen * kQueueStride];
+  __shared__ unsigned char qc[kQueueLen * kQueueStride];
+  const SimParams &P = kp.p;
+  unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 p4 = ldg4(sortedPos + i);
+  float4 v4 = ldg4(sortedVel + i);
+  float3 pos = make_float3(p4.x, p4.y, p4.z), vel = make_float3(v4.x, v4.y, v4.z);
+  float ri = kRadiusFromW ? p4.w : P.particleRadius;
+  int3 g = gridPos(pos.x, pos.y, pos.z, P);
+  if (kRadiusFromW && !(ri <= P.particleRadius)) {  // the culling bound is broken
+    atomicOr(status, (unsigned)kStatusRadiusBound);
+    cull = false;
+  }
+  float3 force = neighbourForceGlobal<kRadiusFromW>(i, n, pos, vel, ri, g, cull, sortedPos,
+                                                    sortedVel, cellStart, cellEnd, P,
+                                                    qj + threadIdx.x, qc + threadIdx.x);
+  finishParticle<kMode, kCollider, kForceOut>(i, n, pos, vel, p4, ri, force, index, newVel,
+                                              forceOut, posOut, hashOut, dt, P);
+}
+
+// ---------------------------------------------------------------------------
+// Bulk copy and mbarrier helpers (PTX).
+
+__device__ __forceinline__ unsigned smemAddr(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbarInit(unsigned long long *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(bar)), "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbarArriveExpectTx(unsigned long long *bar, unsigned bytes) {
+  asm volatile(
+      "{\n\t.reg .b64 st;\n\t"
+      "mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(smemAddr(bar)),
+      "r"(bytes)
+      : "memory");
+}
+
+// Returns true once the barrier's phase `parity` has completed; gives up
+// after kWaitLimit polls.
+__device__ __forceinline__ bool mbarWait(unsigned long long *bar, unsigned parity) {
+  for (unsigned k = 0; k < kWaitLimit; ++k) {
+    unsigned done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smemAddr(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// Global -> shared bulk copy of `bytes` (a multiple of 16, both addresses
+// 16-byte aligned) completing on `bar`.
+__device__ __forceinline__ void bulkCopyG2S(void *dst, const void *src, unsigned bytes,
+                                            unsigned long long *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+      ::"r"(smemAddr(dst)), "l"(src), "r"(bytes), "r"(smemAddr(bar))
+      : "memory");
+}
+
+struct __align__(16) TileSmem {
+  float4 pos[kStageMax];
+  unsigned cs[9][kWinMax];  // window cell ranges, global sorted indices
+  unsigned ce[9][kWinMax];  //   (empty cell: cs = ce = 0)
+  unsigned segStart[9];     // first global index of each row window
+  unsigned segBase[9];      // its offset in pos[]
+  int rowOf[kTileThreads];  // grid row (z*gy + y) of each tile particle
+  int xOf[kTileThreads];    // masked grid x of each tile particle
+  unsigned long long bar;
+  int groupEnd;
+  int staged;
+};
+
+template <int kMode, bool kRadiusFromW, bool kCollider, bool kForceOut>
+__global__ void __launch_bounds__(kTileThreads)
+kCollideTiled(float4 *__restrict__ newVel, float3 *__restrict__ forceOut,
+              const float4 *__restrict__ sortedPos, const float4 *__restrict__ sortedVel,
+              const unsigned *__restrict__ index, const unsigned *__restrict__ cellStart,
+              const unsigned *__restrict__ cellEnd, unsigned n, KParams kp,
+              float4 *__restrict__ posOut, unsigned *__restrict__ hashOut, float dt,
+              unsigned *status) {
+  __shared__ TileSmem sm;
+  __shared__ unsigned qj[kQueueLen * kQueueStride];
+  __shared__ unsigned char qc[kQueueLen * kQueueStride];
+  const SimParams &P = kp.p;
+  const int tid = threadIdx.x;
+  const unsigned p0 = blockIdx.x * kTileThreads;
+  const int count = (int)min((unsigned)kTileThreads, n - p0);
+  const unsigned i = p0 + tid;
+  const bool valid = tid < count;
+  const unsigned gx = P.gridSize[0], gy = P.gridSize[1], gz = P.gridSize[2];
+
+  float4 p4 = make_float4(0.f, 0.f, 0.f, 0.f), v4 = p4;
+  float3 pos = make_float3(0.f, 0.f, 0.f), vel = pos;
+  float ri = P.particleRadius;
+  int3 g = make_int3(0, 0, 0);
+  if (valid) {
+    p4 = ldg4(sortedPos + i);
+    v4 = ldg4(sortedVel + i);
+    pos = make_float3(p4.x, p4.y, p4.z);
+    vel = make_float3(v4.x, v4.y, v4.z);
+    if (kRadiusFromW) ri = p4.w;
+    g = gridPos(pos.x, pos.y, pos.z, P);
+    unsigned y = (unsigned)g.y & (gy - 1u), z = (unsigned)g.z & (gz - 1u);
+    sm.rowOf[tid] = (int)(z * gy + y);
+    sm.xOf[tid] = (int)((unsigned)g.x & (gx - 1u));
+  }
+  if (tid == 0) {
+    mbarInit(&sm.bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+
+  const float cdMono = ri + P.particleRadius;
+  const float cdMonoHi2 = rejectBound(cdMono);
+  float3 force = make_float3(0.0f, 0.0f, 0.0f);
+  bool done = false;
+  unsigned phase = 0;
+  int gStart = 0;
+
+  for (int group = 0; group < kMaxGroups && gStart < count; ++group) {
+    // --- group extent and staging plan (thread 0 and warp 0) ---------------
+    if (tid == 0) {
+      int e = gStart + 1;
+      const int r = sm.rowOf[gStart];
+      while (e < count && sm.rowOf[e] == r) ++e;
+      sm.groupEnd = e;
+    }
+    __syncthreads();
+    const int gEnd = sm.groupEnd;
+    const int rowId = sm.rowOf[gStart];
+    const int xa = sm.xOf[gStart], xb = sm.xOf[gEnd - 1];
+    const int W = xb - xa + 3;
+    // Windows that would wrap around the grid in x, or are too wide, are
+    // not staged (uniform decision for the CTA).
+    const bool stageable = xa >= 1 && xb <= (int)gx - 2 && W <= kWinMax;
+    const int yRow = rowId % (int)gy, zRow = rowId / (int)gy;
+    if (stageable) {
+      // cell-table windows: rows (y + dy, z + dz), cells x in [xa-1, xb+1]
+      for (int t = tid; t < 9 * W; t += kTileThreads) {
+        const int k = t / W, c = t % W;
+        const unsigned h = gridHash(xa - 1 + c, yRow + (k % 3 - 1), zRow + (k / 3 - 1), P);
+        unsigned s = __ldg(cellStart + h), e = 0u;
+        if (s != kEmpty) e = min(__ldg(cellEnd + h), n);
+        else s = 0u;
+        sm.cs[k][c] = s;
+        sm.ce[k][c] = e;
+      }
+      __syncthreads();
+      if (tid < 9) {  // contiguous particle run of each row window
+        const int k = tid;
+        unsigned a = 0u, b = 0u;
+        for (int c = 0; c < W; ++c)
+          if (sm.ce[k][c] > sm.cs[k][c]) { a = sm.cs[k][c]; break; }
+        for (int c = W - 1; c >= 0; --c)
+          if (sm.ce[k][c] > sm.cs[k][c]) { b = sm.ce[k][c]; break; }
+        sm.segStart[k] = a;
+        sm.segBase[k] = b - a;  // length for now
+      }
+      __syncthreads();
+      if (tid == 0) {
+        unsigned total = 0;
+        for (int k = 0; k < 9; ++k) {
+          unsigned len = sm.segBase[k];
+          sm.segBase[k] = total;
+          total += len;
+        }
+        const bool fits = total <= (unsigned)kStageMax;
+        sm.staged = fits ? 1 : 0;
+        if (fits && total > 0) {
+          // make earlier generic reads of pos[] ordered before the async writes
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          mbarArriveExpectTx(&sm.bar, total * 16u);
+          for (int k = 0; k < 9; ++k) {
+            unsigned len = (k < 8 ? sm.segBase[k + 1] : total) - sm.segBase[k];
+            if (len)
+              bulkCopyG2S(&sm.pos[sm.segBase[k]], sortedPos + sm.segStart[k], len * 16u,
+                          &sm.bar);
+          }
+        } else if (fits) {
+          mbarArriveExpectTx(&sm.bar, 0u);  // completes the phase at once
+        }
+      }
+    } else if (tid == 0) {
+      sm.staged = 0;
+    }
+    __syncthreads();
+    const bool staged = stageable && sm.staged;
+    if (staged) {
+      if (!mbarWait(&sm.bar, phase)) {
+        atomicOr(status, (unsigned)kStatusTimeout);
+        // wait (bounded) for the copies in flight before touching the
+        // buffer again or leaving
+        mbarWait(&sm.bar, phase);
+      }
+      phase ^= 1u;
+    }
+
+    // --- pair terms of this group's particles -----------------------------
+    if (valid && tid >= gStart && tid < gEnd) {
+      if (staged) {
+        const int xr = sm.xOf[tid] - (xa - 1);  // window column of the particle
+#pragma unroll 1
+        for (int row = 0; row < 9; row++) {
+          const unsigned base = sm.segBase[row] - sm.segStart[row];
+          auto posOf = [&](unsigned j) { return sm.pos[base + j]; };
+#pragma unroll
+          for (int x = 0; x < 3; x++)
+            cellTerms<kRadiusFromW>(sm.cs[row][xr - 1 + x], sm.ce[row][xr - 1 + x], i, pos,
+                                    vel, ri, cdMono, cdMonoHi2, sortedVel, P, posOf, force);
+        }
+      } else {
+        force = neighbourForceGlobal<kRadiusFromW>(i, n, pos, vel, ri, g, false, sortedPos,
+                                                   sortedVel, cellStart, cellEnd, P,
+                                                   qj + tid, qc + tid);
+      }
+      done = true;
+    }
+    gStart = gEnd;
+    __syncthreads();  // the staged buffers are reused by the next group
+  }
+  if (valid && !done)  // particles past the last staged group
+    force = neighbourForceGlobal<kRadiusFromW>(i, n, pos, vel, ri, g, false, sortedPos,
+                                               sortedVel, cellStart, cellEnd, P, qj + tid,
+                                               qc + tid);
+  if (valid)
+    finishParticle<kMode, kCollider, kForceOut>(i, n, pos, vel, p4, ri, force, index, newVel,
+                                                forceOut, posOut, hashOut, dt, P);
+}
+
+template <int kMode, bool kRadiusFromW, bool kCollider, bool kForceOut>
+void launchT(bool tiled, bool cull, unsigned n, float4 *newVel, float3 *force,
+             const float4 *sp, const float4 *sv, const unsigned *index, const unsigned *cs,
+             const unsigned *ce, const KParams &kp, float4 *posOut, unsigned *hashOut,
+             float dt) {
+  unsigned blocks = (n + 127) / 128;
+  if (tiled)
+    kCollideTiled<kMode, kRadiusFromW, kCollider, kForceOut>
+        <<<blocks, kTileThreads, 0, curStream()>>>(newVel, force, sp, sv, index, cs, ce, n,
+                                                   kp, posOut, hashOut, dt, ctx().dStatus);
+  else
+    kCollideGlobal<kMode, kRadiusFromW, kCollider, kForceOut>
+        <<<blocks, 128, 0, curStream()>>>(newVel, force, sp, sv, index, cs, ce, n, kp,
+                                          posOut, hashOut, dt, cull, ctx().dStatus);
+}
+
+int g_collidePath = -1;  // -1 auto, 0 global, 1 tiled (fcdemSetCollidePath)
+bool g_cullCells = true;  // fcdemSetCellCulling
+
+}  // namespace
+
+void launchCollide(int mode, bool collider, float4 *newVel, float3 *force,
+                   const float4 *sp, const float4 *sv, const unsigned *index,
+                   const unsigned *cs, const unsigned *ce, unsigned n, const KParams &kp,
+                   float4 *posOut, unsigned *hashOut, float dt) {
+  if (n == 0) return;
+  // The bulk copies need 16-byte aligned positions; the tiled kernel is
+  // opt-in (fcdemSetCollidePath(1)): the culled global kernel is faster.
+  bool tiled = g_collidePath == 1 && ((uintptr_t)sp & 15u) == 0;
+  // Culling is exact when every grid dimension is >= 3 and the largest
+  // contact distance 2 * particleRadius fits in the smallest cell.
+  const SimParams &P = kp.p;
+  float minCell = fminf(P.cellSize[0], fminf(P.cellSize[1], P.cellSize[2]));
+  bool cull = g_cullCells && P.gridSize[0] >= 3 && P.gridSize[1] >= 3 &&
+              P.gridSize[2] >= 3 && 2.0f * P.particleRadius <= minCell &&
+              P.particleRadius > 0.0f;
+  const bool w = kp.radiusFromW != 0;
+  const bool fo = force != nullptr;
+#define FCDEM_COLLIDE_CASE(M, W, C, F)                                                  \
+  if (mode == M && w == W && collider == C && fo == F) {                                \
+    launchT<M, W, C, F>(tiled, cull, n, newVel, force, sp, sv, index, cs, ce, kp,       \
+                        posOut, hashOut, dt);                                           \
+    launchOk();                                                                         \
+    return;                                                                             \
+  }
+  FCDEM_COLLIDE_CASE(0, false, true, false)
+  FCDEM_COLLIDE_CASE(0, true, true, false)
+  FCDEM_COLLIDE_CASE(0, false, false, false)
+  FCDEM_COLLIDE_CASE(0, true, false, false)
+  FCDEM_COLLIDE_CASE(0, false, false, true)
+  FCDEM_COLLIDE_CASE(0, true, false, true)
+  FCDEM_COLLIDE_CASE(0, false, true, true)
+  FCDEM_COLLIDE_CASE(0, true, true, true)
+  FCDEM_COLLIDE_CASE(1, false, true, false)
+  FCDEM_COLLIDE_CASE(1, true, true, false)
+#undef FCDEM_COLLIDE_CASE
+  setError(FCDEM_ERR_INVALID_VALUE);
+}
+
+}  // namespace fcdem
+
+extern "C" void fcdemSetCollidePath(int path) {
+  fcdem::g_collidePath = (path == 0 || path == 1) ? path : -1;
+}
+
+extern "C" void fcdemSetCellCulling(int on) { fcdem::g_cullCells = on != 0; }

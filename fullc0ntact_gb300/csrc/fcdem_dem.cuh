@@ -81,8 +81,22 @@ __device__ __forceinline__ float3 contactTerm(float3 rel, float dist, float cd,
   return f;
 }
 
-__device__ __forceinline__ float pairDist(float3 rel) {
-  return sqrtf(rel.x * rel.x + rel.y * rel.y + rel.z * rel.z);
+// |rel|^2 with the operations of length() (cutil_math.cuh: sqrtf(dot(v,v))),
+// so that sqrtf(pairDist2(rel)) is the reference's distance bit for bit.
+__device__ __forceinline__ float pairDist2(float3 rel) {
+  return rel.x * rel.x + rel.y * rel.y + rel.z * rel.z;
+}
+
+__device__ __forceinline__ float pairDist(float3 rel) { return sqrtf(pairDist2(rel)); }
+
+// Squared-distance bound for the contact test: d2 >= rejectBound(cd) implies
+// sqrtf(d2) >= cd, so such a pair cannot pass `dist < cd` and is skipped
+// without the (multi-instruction) IEEE square root.  Proof: the computed
+// bound is >= cd^2 (1 - 2^-24)^2 (1 + 2.4e-6) > cd^2 (1 + 2.2e-6), hence
+// sqrt(d2) > cd (1 + 1.1e-6) and the correctly rounded sqrtf(d2) > cd.
+// Pairs below the bound take the exact test, so results are unchanged.
+__device__ __forceinline__ float rejectBound(float cd) {
+  return (cd * cd) * 1.0000025f;
 }
 
 }  // namespace fcdem

@@ -30,6 +30,7 @@ static_assert(offsetof(SimParams, boundaryDamping) == 100, "layout");
 enum : unsigned {
   kStatusTimeout = 1u,   // a bounded spin-wait gave up
   kStatusKeyRange = 2u,  // a sort key had bits above the sorted width
+  kStatusRadiusBound = 4u,  // radius-from-w mode: a radius above particleRadius
 };
 
 // Everything a kernel needs from the parameter block, passed by value so
@@ -91,5 +92,13 @@ void radixSortPairs(Context &c, unsigned *keys, unsigned *vals, unsigned n,
 
 // Cell-table fill (cellStart = 0xffffffff).  Defined in fcdem_stages.cu.
 void fillU32(Context &c, unsigned *p, size_t count, unsigned value);
+
+// collide (particles_kernel.cu:185-293), defined in fcdem_collide.cu.
+// mode 0: newVel[index[i]] = (v + F, 0).  mode 1: also the next update's
+// integrate and calcHash (posOut, hashOut).  force != nullptr also stores F.
+void launchCollide(int mode, bool collider, float4 *newVel, float3 *force,
+                   const float4 *sp, const float4 *sv, const unsigned *index,
+                   const unsigned *cs, const unsigned *ce, unsigned n,
+                   const KParams &kp, float4 *posOut, unsigned *hashOut, float dt);
 
 }  // namespace fcdem

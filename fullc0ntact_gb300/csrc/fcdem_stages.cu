@@ -117,144 +117,7 @@ kReorder(unsigned *__restrict__ cellStart, unsigned *__restrict__ cellEnd,
   sortedVel[i] = ldg4(oldVel + s);
 }
 
-// ---------------------------------------------------------------------------
-// collide (particles_kernel.cu:185-293).  One thread per sorted particle.
-// The neighbour cells are visited in the reference's z, y, x order and the
-// particles of a cell in ascending sorted index; each cell's terms are summed
-// into a cell subtotal that is then added to the particle total, as
-// collideCell/collideD do, so the float sums are the reference's.  The
-// neighbour's velocity is only loaded for pairs in contact.
-//
-// kMode 0: write newVel[index[i]] = (v + F, 0) (the reference).
-// kMode 1: additionally integrate the particle for the next step and write
-//          pos/vel/hash/index of the next step (fcdemUpdate).
-template <int kMode, bool kRadiusFromW, bool kCollider, bool kForceOut>
-__global__ void __launch_bounds__(128)
-kCollide(float4 *__restrict__ newVel, float3 *__restrict__ forceOut,
-         const float4 *__restrict__ sortedPos,
-         const float4 *__restrict__ sortedVel,
-         const unsigned *__restrict__ index,
-         const unsigned *__restrict__ cellStart,
-         const unsigned *__restrict__ cellEnd, unsigned n, KParams kp,
-         float4 *__restrict__ posOut, unsigned *__restrict__ hashOut, float dt) {
-  const SimParams &P = kp.p;
-  unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  float4 p4 = ldg4(sortedPos + i);
-  float4 v4 = ldg4(sortedVel + i);
-  float3 pos = make_float3(p4.x, p4.y, p4.z);
-  float3 vel = make_float3(v4.x, v4.y, v4.z);
-  float ri = kRadiusFromW ? p4.w : P.particleRadius;
-  int3 g = gridPos(pos.x, pos.y, pos.z, P);
-
-  float3 force = make_float3(0.0f, 0.0f, 0.0f);
-#pragma unroll 1
-  for (int z = -1; z <= 1; z++) {
-#pragma unroll 1
-    for (int y = -1; y <= 1; y++) {
-#pragma unroll
-      for (int x = -1; x <= 1; x++) {
-        unsigned h = gridHash(g.x + x, g.y + y, g.z + z, P);
-        unsigned start = __ldg(cellStart + h);
-        float3 cf = make_float3(0.0f, 0.0f, 0.0f);
-        if (start != kEmpty) {
-          unsigned end = min(__ldg(cellEnd + h), n);
-          for (unsigned j = start; j < end; j++) {
-            if (j == i) continue;
-            float4 q4 = ldg4(sortedPos + j);
-            float3 rel = make_float3(q4.x - pos.x, q4.y - pos.y, q4.z - pos.z);
-            float dist = pairDist(rel);
-            float cd = ri + (kRadiusFromW ? q4.w : P.particleRadius);
-            if (dist < cd) {
-              float4 w4 = ldg4(sortedVel + j);
-              float3 f = contactTerm(rel, dist, cd, vel,
-                                     make_float3(w4.x, w4.y, w4.z),
-                                     P.attraction, P);
-              cf.x = cf.x + f.x;
-              cf.y = cf.y + f.y;
-              cf.z = cf.z + f.z;
-            }
-          }
-        }
-        force.x = force.x + cf.x;
-        force.y = force.y + cf.y;
-        force.z = force.z + cf.z;
-      }
-    }
-  }
-  if (kCollider) {  // particles_kernel.cu:288, the collider sphere
-    float3 cpos = make_float3(P.colliderPos[0], P.colliderPos[1], P.colliderPos[2]);
-    float3 rel = make_float3(cpos.x - pos.x, cpos.y - pos.y, cpos.z - pos.z);
-    float dist = pairDist(rel);
-    float cd = ri + P.colliderRadius;
-    if (dist < cd) {
-      float3 f = contactTerm(rel, dist, cd, vel, make_float3(0.0f, 0.0f, 0.0f),
-                             0.0f, P);
-      force.x = force.x + f.x;
-      force.y = force.y + f.y;
-      force.z = force.z + f.z;
-    }
-  }
-  unsigned o = __ldg(index + i);
-  if (o >= n) return;  // not a permutation of 0..n-1: nothing to write to
-  float3 nv = make_float3(vel.x + force.x, vel.y + force.y, vel.z + force.z);
-  if (kForceOut) forceOut[o] = force;
-  if (kMode == 0) {
-    newVel[o] = make_float4(nv.x, nv.y, nv.z, 0.0f);
-  } else {
-    // The next update's integrate and calcHash for particle o: its position
-    // is sortedPos[i] (the reorder gathered pos[o]), its velocity nv with
-    // w = 0 as collide leaves it.
-    integrateOne(pos, nv, dt, ri, P);
-    posOut[o] = make_float4(pos.x, pos.y, pos.z, p4.w);
-    newVel[o] = make_float4(nv.x, nv.y, nv.z, 0.0f);
-    // The next calcHash.  Its index[o] = o is not stored: this kernel still
-    // reads the index array, and the next sort generates identity values.
-    int3 gn = gridPos(pos.x, pos.y, pos.z, P);
-    hashOut[o] = gridHash(gn.x, gn.y, gn.z, P);
-  }
-}
-
-template <int kMode, bool kRadiusFromW, bool kCollider, bool kForceOut>
-static void launchCollideT(unsigned blocks, float4 *newVel, float3 *force,
-                           const float4 *sp, const float4 *sv,
-                           const unsigned *index, const unsigned *cs,
-                           const unsigned *ce, unsigned n, const KParams &kp,
-                           float4 *posOut, unsigned *hashOut, float dt) {
-  kCollide<kMode, kRadiusFromW, kCollider, kForceOut>
-      <<<blocks, 128, 0, curStream()>>>(newVel, force, sp, sv, index, cs, ce, n,
-                                         kp, posOut, hashOut, dt);
-}
-
-void launchCollide(int mode, bool collider, float4 *newVel, float3 *force,
-                   const float4 *sp, const float4 *sv, const unsigned *index,
-                   const unsigned *cs, const unsigned *ce, unsigned n,
-                   const KParams &kp, float4 *posOut, unsigned *hashOut,
-                   float dt) {
-  if (n == 0) return;
-  unsigned blocks = (n + 127) / 128;
-  bool w = kp.radiusFromW != 0;
-  bool fo = force != nullptr;
-#define FCDEM_COLLIDE_CASE(M, W, C, F)                                        \
-  if (mode == M && w == W && collider == C && fo == F) {                      \
-    launchCollideT<M, W, C, F>(blocks, newVel, force, sp, sv, index, cs, ce,  \
-                               n, kp, posOut, hashOut, dt);                    \
-    launchOk();                                                               \
-    return;                                                                   \
-  }
-  FCDEM_COLLIDE_CASE(0, false, true, false)
-  FCDEM_COLLIDE_CASE(0, true, true, false)
-  FCDEM_COLLIDE_CASE(0, false, false, false)
-  FCDEM_COLLIDE_CASE(0, true, false, false)
-  FCDEM_COLLIDE_CASE(0, false, false, true)
-  FCDEM_COLLIDE_CASE(0, true, false, true)
-  FCDEM_COLLIDE_CASE(0, false, true, true)
-  FCDEM_COLLIDE_CASE(0, true, true, true)
-  FCDEM_COLLIDE_CASE(1, false, true, false)
-  FCDEM_COLLIDE_CASE(1, true, true, false)
-#undef FCDEM_COLLIDE_CASE
-  setError(FCDEM_ERR_INVALID_VALUE);
-}
+// collide lives in fcdem_collide.cu (launchCollide).
 
 void launchIntegrateHash(float4 *pos, float4 *vel, float dt, unsigned *hash,
                          unsigned *index, unsigned n, const KParams &kp) {

@@ -134,6 +134,7 @@ void collide(float *newVel, float *sortedPos, float *sortedVel,
 #define FCDEM_ERR_DEVICE_TIMEOUT    5  /* a bounded device-side wait expired  */
 #define FCDEM_ERR_KEY_RANGE         6  /* sort key above the grid's key width */
 #define FCDEM_ERR_ALLOC             7  /* device scratch allocation failed    */
+#define FCDEM_ERR_RADIUS_BOUND      8  /* a radius above particleRadius (w mode) */
 
 /* Returns and clears the first error recorded since the last call.  It
  * synchronises the library stream so that device-side status words (bounded
@@ -149,8 +150,15 @@ void fcdemSetStream(void *stream);
  * the reference.  1: the radius of particle i is pos[i].w (polydisperse
  * scenes); collide uses radiusA = r_i, radiusB = r_j, which
  * collideSpheres(particles_kernel.cu:185-218) accepts but collideCell never
- * passes, and integrate clamps with r_i. */
+ * passes, and integrate clamps with r_i.  In this mode particleRadius must be
+ * an upper bound of every radius (collide culls cells with it); a larger
+ * radius records FCDEM_ERR_RADIUS_BOUND. */
 void fcdemSetRadiusMode(int radiusFromW);
+
+/* Cell culling in collide (default on): neighbour cells whose box is farther
+ * than the largest contact distance are not scanned.  Results are identical
+ * either way; the switch exists to measure and test that. */
+void fcdemSetCellCulling(int on);
 
 /* Library version string. */
 const char *fcdemVersion(void);
@@ -165,6 +173,10 @@ void fcdemUpdate(float *pos, float *vel, float *sortedPos, float *sortedVel,
                  uint *gridParticleHash, uint *gridParticleIndex,
                  uint *cellStart, uint *cellEnd, float deltaTime,
                  uint numParticles, uint numCells, uint steps);
+
+/* Collide kernel selection: -1 (default) automatic, 0 the global-read
+ * kernel, 1 the shared-memory tiled kernel.  Both give identical results. */
+void fcdemSetCollidePath(int path);
 
 /* Number of kernels this library has launched in this process. */
 unsigned long long fcdemGetLaunchCount(void);
