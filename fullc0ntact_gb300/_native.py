@@ -41,6 +41,7 @@ _SIGS = {
     "integrateSystem": (None, [vp, vp, C.c_float, u32]),
     "calcHash": (None, [vp, vp, vp, C.c_int]),
     "sortParticles": (None, [vp, vp, u32]),
+    "fcdemSortParticlesNoAlloc": (None, [vp, vp, u32]),
     "reorderDataAndFindCellStart": (None, [vp] * 8 + [u32, u32]),
     "collide": (None, [vp] * 6 + [u32, u32]),
     # extensions

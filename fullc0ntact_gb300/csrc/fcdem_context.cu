@@ -97,6 +97,17 @@ Context &ctx() {
   return c;
 }
 
+const Context *ctxIfCreated() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (dev < 0 || dev >= kMaxDevices) return nullptr;
+  const Context &c = g_ctx[dev];
+  return c.device >= 0 ? &c : nullptr;
+}
+
 void *scratch(Context &c, size_t bytes) {
   if (bytes <= c.scratchBytes) return c.scratch;
   // Work already queued (on any stream) may still use the old block.

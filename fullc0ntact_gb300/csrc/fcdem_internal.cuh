@@ -54,6 +54,9 @@ struct Context {
 
 // The context of the calling thread's current device (created on first use).
 Context &ctx();
+// The context of the current device if one has been created, else nullptr;
+// never creates one (creating one allocates its device status word).
+const Context *ctxIfCreated();
 // The stream this host thread issues work on (fcdemSetStream; default: the
 // legacy default stream, as the reference).
 cudaStream_t curStream();

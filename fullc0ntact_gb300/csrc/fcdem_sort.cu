@@ -11,6 +11,8 @@
 // Every look-back spin is bounded: after kSpinLimit polls the CTA records
 // kStatusTimeout in the device status word and carries on, so a fault in the
 // protocol turns into an error the host reads, never into a hung GPU.
+#include <mutex>
+
 #include "fcdem_internal.cuh"
 
 namespace fcdem {
@@ -307,4 +309,124 @@ void radixSortPairs(Context &c, unsigned *keys, unsigned *vals, unsigned n,
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// sortParticles without allocation (fcdemSortParticlesNoAlloc).
+//
+// Some callers must not have the library allocate device memory: code that
+// records work into a CUDA graph (a cudaMalloc during stream capture breaks
+// the capture), hosts that own every byte of device memory through their own
+// pool and forbid hidden allocations, and loops running close to the memory
+// limit.  sortParticles grows its scratch with cudaMalloc on first use; this
+// variant uses a fixed scratch array in the library's static device memory
+// instead, sized for kNoAllocMaxParticles particles.  That array exists on
+// every GPU that loads the library, for the life of the process.
+
+namespace {
+
+constexpr unsigned kNoAllocMaxParticles = 1u << 20;
+constexpr size_t kNoAllocArr = (size_t)kNoAllocMaxParticles * 4;  // one key/value array
+constexpr unsigned kNoAllocMaxTiles = (kNoAllocMaxParticles + kTile - 1) / kTile;
+constexpr size_t kNoAllocHist = (kMaxPasses * kRadix * 4 + kMaxPasses * 4 + 255) & ~(size_t)255;
+constexpr size_t kNoAllocLookback = (size_t)kMaxPasses * kNoAllocMaxTiles * kRadix * 4;
+constexpr size_t kNoAllocStatus = 256;
+constexpr size_t kNoAllocBytes =
+    4 * kNoAllocArr + kNoAllocHist + kNoAllocLookback + kNoAllocStatus;  // ~17 MB
+
+// The scratch itself.  In host code this name is only a host-side stand-in
+// for the device array, not a device address: the kernels get the address
+// that cudaGetSymbolAddress returns for the current device.
+static __device__ __align__(256) unsigned char g_noAllocScratch[kNoAllocBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noAllocMutex;
+unsigned char *g_noAllocPtr[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch on the current device, looked up once per
+// device (with that device current) and cached; nullptr on failure.
+unsigned char *noAllocScratch() {
+  int dev = 0;
+  if (!cudaOk(cudaGetDevice(&dev))) return nullptr;
+  if (dev < 0 || dev >= kNoAllocMaxDevices) { setError(FCDEM_ERR_INVALID_VALUE); return nullptr; }
+  std::lock_guard<std::mutex> lock(g_noAllocMutex);
+  if (!g_noAllocPtr[dev]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noAllocScratch);
+    if (e != cudaSuccess || !p) {
+      cudaGetLastError();
+      setError(FCDEM_ERR_CUDA);
+      return nullptr;
+    }
+    g_noAllocPtr[dev] = (unsigned char *)p;
+  }
+  return g_noAllocPtr[dev];
+}
+
+}  // namespace
+
 }  // namespace fcdem
+
+extern "C" void fcdemSortParticlesNoAlloc(uint *dGridParticleHash, uint *dGridParticleIndex,
+                                          uint numParticles) {
+  using namespace fcdem;
+  const unsigned n = numParticles;
+  if (n < 2) return;
+  if (!dGridParticleHash || !dGridParticleIndex) { setError(FCDEM_ERR_INVALID_VALUE); return; }
+  if (n > kNoAllocMaxParticles) {  // the fixed scratch does not fit more
+    setError(FCDEM_ERR_INVALID_VALUE);
+    return;
+  }
+  unsigned char *s = noAllocScratch();
+  if (!s) return;
+  // Same key width as sortParticles; the existing context is used only if
+  // the caller already created one (setParameters), never created here.
+  const Context *c = ctxIfCreated();
+  int bits = (c && c->haveParams) ? keyBits(c->params.numCells) : 32;
+  const int passes = (bits + kRadixBits - 1) / kRadixBits;
+  const unsigned tiles = (n + kTile - 1) / kTile;
+  unsigned *keys = dGridParticleHash, *vals = dGridParticleIndex;
+  unsigned *kB = (unsigned *)s, *vB = (unsigned *)(s + kNoAllocArr);
+  unsigned *kC = (unsigned *)(s + 2 * kNoAllocArr), *vC = (unsigned *)(s + 3 * kNoAllocArr);
+  unsigned char *meta = s + 4 * kNoAllocArr;
+  unsigned *hist = (unsigned *)meta;
+  unsigned *counters = hist + kMaxPasses * kRadix;
+  unsigned *lookback = (unsigned *)(meta + kNoAllocHist);
+  unsigned *status = (c && c->dStatus) ? c->dStatus
+                                       : (unsigned *)(meta + kNoAllocHist + kNoAllocLookback);
+  cudaStream_t st = curStream();
+  // The array keeps whatever the previous call left; the histograms, tile
+  // counters and look-back flags must start at zero.
+  if (!cudaOk(cudaMemsetAsync(meta, 0, kNoAllocHist + (size_t)passes * tiles * kRadix * 4,
+                              st)))
+    return;
+  unsigned upBlocks = (n + kThreads * 16 - 1) / (kThreads * 16);
+  if (upBlocks > 152u * 4u) upBlocks = 152u * 4u;
+  kUpsweep<<<upBlocks, kThreads, 0, st>>>(keys, n, passes, bits, hist, status);
+  if (!launchOk()) return;
+  unsigned *srcK = keys, *srcV = vals;
+  for (int p = 0; p < passes; ++p) {
+    unsigned *dstK, *dstV;
+    if (passes == 1) {
+      dstK = kB; dstV = vB;
+    } else if (passes % 2 == 1 && p < 3) {
+      if (p == 0) { dstK = kB; dstV = vB; }
+      else if (p == 1) { dstK = kC; dstV = vC; }
+      else { dstK = keys; dstV = vals; }
+    } else {
+      bool toB = (srcK == keys);
+      dstK = toB ? kB : keys;
+      dstV = toB ? vB : vals;
+    }
+    kOnesweep<<<tiles, kThreads, 0, st>>>(srcK, srcV, dstK, dstV, n, p * kRadixBits,
+                                         hist + p * kRadix,
+                                         lookback + (size_t)p * tiles * kRadix, counters + p,
+                                         status);
+    if (!launchOk()) return;
+    srcK = dstK;
+    srcV = dstV;
+  }
+  if (srcK != keys) {
+    cudaOk(cudaMemcpyAsync(keys, srcK, (size_t)n * 4, cudaMemcpyDeviceToDevice, st));
+    cudaOk(cudaMemcpyAsync(vals, srcV, (size_t)n * 4, cudaMemcpyDeviceToDevice, st));
+  }
+}

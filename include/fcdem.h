@@ -111,6 +111,24 @@ void calcHash(uint *gridParticleHash, uint *gridParticleIndex, float *pos,
 void sortParticles(uint *dGridParticleHash, uint *dGridParticleIndex,
                    uint numParticles);
 
+/* No counterpart in the reference.  The same sort as sortParticles, for
+ * callers that must not have the library allocate device memory: code being
+ * recorded into a CUDA graph (a cudaMalloc during stream capture invalidates
+ * the capture), hosts whose own pool owns all device memory, and loops run
+ * near the memory limit.  sortParticles allocates its scratch on first use;
+ * this entry point allocates nothing and uses a fixed ~17 MB scratch array in
+ * the library's static device memory, present on every GPU that loads the
+ * library until the process exits.
+ *   - At most 1,048,576 particles; more records FCDEM_ERR_INVALID_VALUE and
+ *     leaves the arrays untouched.
+ *   - Its first call on a device looks up that array's device address (with
+ *     the device current); make that first call before any stream capture.
+ *   - Every call shares the one array: calls that overlap on the GPU (other
+ *     streams, other host threads) race and corrupt each other's results.
+ *     Issue them in order on one stream. */
+void fcdemSortParticlesNoAlloc(uint *dGridParticleHash, uint *dGridParticleIndex,
+                               uint numParticles);
+
 /* particleSystem.cu:246-285 + particles_kernel.cu:119-182 */
 void reorderDataAndFindCellStart(uint *cellStart, uint *cellEnd,
                                  float *sortedPos, float *sortedVel,
