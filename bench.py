@@ -239,6 +239,9 @@ def run_ours(args):
     sc = load_scene(args.n)
     n = sc["pos"].shape[0]
     ds = dem.DeviceScene(sc, f"cuda:{dev}")
+    # project autotuner: the sort's block shape for this size (setup, untimed)
+    tuned_ms = C.c_float()
+    sort_cfg = lib.fcdemAutotuneSort(n, ds.num_cells, C.byref(tuned_ms))
 
     def barrier():
         if world > 1:
@@ -336,6 +339,7 @@ def run_ours(args):
             "data": "synthetic (seeded packing)",
             "config": {"workload": WORKLOAD, "n": n, "grid": 256, "cells": ncell,
                        "occupied_cells": occupied, "step": "fcdemUpdate (fused update)",
+                       "sort_config": sort_cfg,
                        "l2": "inputs larger than L2 (no flush)",
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,

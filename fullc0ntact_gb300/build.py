@@ -20,6 +20,7 @@ SOURCES = [
     "fcdem_stages.cu",
     "fcdem_sort.cu",
     "fcdem_collide.cu",
+    "fcdem_count.cu",
     "fcdem_host.cpp",
 ]
 

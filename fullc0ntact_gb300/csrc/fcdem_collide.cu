@@ -70,8 +70,7 @@ template <int kMode, bool kCollider, bool kForceOut>
 __device__ __forceinline__ void finishParticle(
     unsigned i, unsigned n, float3 pos, float3 vel, float4 p4, float ri,
     float3 force, const unsigned *__restrict__ index, float4 *__restrict__ newVel,
-    float3 *__restrict__ forceOut, float4 *__restrict__ posOut,
-    unsigned *__restrict__ hashOut, float dt, const SimParams &P) {
+    const CollideOut &out, const SimParams &P) {
   if (kCollider) {
     float3 rel = make_float3(P.colliderPos[0] - pos.x, P.colliderPos[1] - pos.y,
                              P.colliderPos[2] - pos.z);
@@ -84,22 +83,36 @@ __device__ __forceinline__ void finishParticle(
       force.z = force.z + f.z;
     }
   }
+  float3 nv = make_float3(vel.x + force.x, vel.y + force.y, vel.z + force.z);
+  if (kMode == 2) {
+    // Counting pipeline: the next update's integrate and calcHash, kept at
+    // sorted slot i (the next step's scatter reads them in this order).
+    integrateOne(pos, nv, out.dt, ri, P);
+    out.posOut[i] = make_float4(pos.x, pos.y, pos.z, p4.w);
+    newVel[i] = make_float4(nv.x, nv.y, nv.z, 0.0f);
+    int3 gn = gridPos(pos.x, pos.y, pos.z, P);
+    const unsigned h = gridHash(gn.x, gn.y, gn.z, P);
+    out.hashOut[i] = h;
+    out.rankOut[i] = atomicAdd(out.cnt + h, 1u);
+    return;
+  }
   unsigned o = __ldg(index + i);
   if (o >= n) return;  // not a permutation of 0..n-1: nothing to write to
-  float3 nv = make_float3(vel.x + force.x, vel.y + force.y, vel.z + force.z);
-  if (kForceOut) forceOut[o] = force;
-  if (kMode == 0) {
+  if (kForceOut) out.force[o] = force;
+  if (kMode == 0 || kMode == 3) {
     newVel[o] = make_float4(nv.x, nv.y, nv.z, 0.0f);
+    if (kMode == 3) out.posOut[o] = p4;  // the state back in particle order
   } else {
+    const float dt = out.dt;
     // The next update's integrate and calcHash for particle o: its position
     // is sortedPos[i] (the reorder gathered pos[o]) and its velocity nv with
     // w = 0 as collide leaves it.  index[o] = o is not stored (this kernel
     // still reads the index array); the next sort generates identity values.
     integrateOne(pos, nv, dt, ri, P);
-    posOut[o] = make_float4(pos.x, pos.y, pos.z, p4.w);
+    out.posOut[o] = make_float4(pos.x, pos.y, pos.z, p4.w);
     newVel[o] = make_float4(nv.x, nv.y, nv.z, 0.0f);
     int3 gn = gridPos(pos.x, pos.y, pos.z, P);
-    hashOut[o] = gridHash(gn.x, gn.y, gn.z, P);
+    out.hashOut[o] = gridHash(gn.x, gn.y, gn.z, P);
   }
 }
 
@@ -161,12 +174,11 @@ constexpr int kQueueStride = 128;
 // contact of a later cell arrives.  Cells without contacts would add +0.0,
 // which leaves a sum that started at +0.0 unchanged, so the result is the
 // reference's cell-by-cell sum.
-template <bool kRadiusFromW>
+template <bool kRadiusFromW, bool kPrefix>
 __device__ __forceinline__ float3 neighbourForceGlobal(
     unsigned i, unsigned n, float3 pos, float3 vel, float ri, int3 g, bool cull,
     const float4 *__restrict__ sortedPos, const float4 *__restrict__ sortedVel,
-    const unsigned *__restrict__ cellStart, const unsigned *__restrict__ cellEnd,
-    const SimParams &P, unsigned *qj, unsigned char *qc) {
+    const CellRanges &cells, const SimParams &P, unsigned *qj, unsigned char *qc) {
   const float cdMono = ri + P.particleRadius;
   const float cdMonoHi2 = rejectBound(cdMono);
   // largest contact distance: r_i + particleRadius (in the radius-from-w
@@ -203,23 +215,58 @@ __device__ __forceinline__ float3 neighbourForceGlobal(
     }
     qn = 0;
   };
+  // queue a near partner j of neighbour cell `cell` (0..26)
+  auto scanRange = [&](unsigned a, unsigned b, int cellA, unsigned m1, unsigned m2) {
+    // cells cellA, cellA+1, cellA+2 hold [a, m1), [m1, m2), [m2, b)
+    for (unsigned j = a; j < b; j++) {
+      float4 q4 = ldg4(sortedPos + j);
+      float3 rel = make_float3(q4.x - pos.x, q4.y - pos.y, q4.z - pos.z);
+      float d2 = pairDist2(rel);
+      float hi2 = kRadiusFromW ? rejectBound(ri + q4.w) : cdMonoHi2;
+      if (d2 < hi2 && j != i) {
+        if (qn == kQueueLen) drain();
+        qj[qn * kQueueStride] = j;
+        qc[qn * kQueueStride] = (unsigned char)(cellA + (j >= m1) + (j >= m2));
+        ++qn;
+      }
+    }
+  };
 #pragma unroll 1
   for (int row = 0; row < 9; row++) {
     const int z = row / 3 - 1, y = row % 3 - 1;
     const float rowD2 = CellCull::pick(z, cc.zl, cc.zh) + CellCull::pick(y, cc.yl, cc.yh);
     if (rowD2 > cullR2) continue;
+    const bool useL = rowD2 + CellCull::pick(-1, cc.xl, cc.xh) <= cullR2;
+    const bool useR = rowD2 + CellCull::pick(1, cc.xl, cc.xh) <= cullR2;
+    if (kPrefix) {
+      const unsigned gxm = P.gridSize[0] - 1u;
+      const unsigned xm = (unsigned)(g.x) & gxm;
+      if (xm >= 1u && xm < gxm) {
+        // no x wrap: the row's three cells are consecutive hashes, one range
+        const unsigned h0 = gridHash(g.x - 1, g.y + y, g.z + z, P);
+        const unsigned o0 = __ldg(cells.off + h0), o1 = __ldg(cells.off + h0 + 1);
+        const unsigned o2 = __ldg(cells.off + h0 + 2), o3 = __ldg(cells.off + h0 + 3);
+        const unsigned a = useL ? o0 : o1, b = min(useR ? o3 : o2, n);
+        scanRange(a, b, row * 3, o1, o2);
+        continue;
+      }
+    }
     unsigned h[3], start[3], end[3];
 #pragma unroll
     for (int x = 0; x < 3; x++) {
       start[x] = kEmpty;
       if (rowD2 + CellCull::pick(x - 1, cc.xl, cc.xh) <= cullR2) {
         h[x] = gridHash(g.x + x - 1, g.y + y, g.z + z, P);
-        start[x] = __ldg(cellStart + h[x]);
+        start[x] = __ldg((kPrefix ? cells.off : cells.start) + h[x]);
       }
     }
 #pragma unroll
-    for (int x = 0; x < 3; x++)
-      end[x] = start[x] != kEmpty ? min(__ldg(cellEnd + h[x]), n) : 0u;
+    for (int x = 0; x < 3; x++) {
+      if (kPrefix)  // off[h] .. off[h+1]; empty when equal
+        end[x] = start[x] != kEmpty ? min(__ldg(cells.off + h[x] + 1), n) : 0u;
+      else
+        end[x] = start[x] != kEmpty ? min(__ldg(cells.end + h[x]), n) : 0u;
+    }
 #pragma unroll
     for (int x = 0; x < 3; x++) {
       const unsigned b = end[x];
@@ -244,14 +291,12 @@ __device__ __forceinline__ float3 neighbourForceGlobal(
   return force;
 }
 
-template <int kMode, bool kRadiusFromW, bool kCollider, bool kForceOut>
+template <int kMode, bool kRadiusFromW, bool kCollider, bool kForceOut, bool kPrefix>
 __global__ void __launch_bounds__(128)
-kCollideGlobal(float4 *__restrict__ newVel, float3 *__restrict__ forceOut,
-               const float4 *__restrict__ sortedPos, const float4 *__restrict__ sortedVel,
-               const unsigned *__restrict__ index, const unsigned *__restrict__ cellStart,
-               const unsigned *__restrict__ cellEnd, unsigned n, KParams kp,
-               float4 *__restrict__ posOut, unsigned *__restrict__ hashOut, float dt,
-               bool cull, unsigned *status) {
+kCollideGlobal(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
+               const float4 *__restrict__ sortedVel, const unsigned *__restrict__ index,
+               CellRanges cells, unsigned n, KParams kp, CollideOut out, bool cull,
+               unsigned *status) {
   __shared__ unsigned qj[kQueueLen * kQueueStride];
   __shared__ unsigned char qc[kQueueLen * kQueueStride];
   const SimParams &P = kp.p;
@@ -266,11 +311,11 @@ kCollideGlobal(float4 *__restrict__ newVel, float3 *__restrict__ forceOut,
     atomicOr(status, (unsigned)kStatusRadiusBound);
     cull = false;
   }
-  float3 force = neighbourForceGlobal<kRadiusFromW>(i, n, pos, vel, ri, g, cull, sortedPos,
-                                                    sortedVel, cellStart, cellEnd, P,
-                                                    qj + threadIdx.x, qc + threadIdx.x);
+  float3 force = neighbourForceGlobal<kRadiusFromW, kPrefix>(
+      i, n, pos, vel, ri, g, cull, sortedPos, sortedVel, cells, P, qj + threadIdx.x,
+      qc + threadIdx.x);
   finishParticle<kMode, kCollider, kForceOut>(i, n, pos, vel, p4, ri, force, index, newVel,
-                                              forceOut, posOut, hashOut, dt, P);
+                                              out, P);
 }
 
 // ---------------------------------------------------------------------------
@@ -335,12 +380,11 @@ struct __align__(16) TileSmem {
 
 template <int kMode, bool kRadiusFromW, bool kCollider, bool kForceOut>
 __global__ void __launch_bounds__(kTileThreads)
-kCollideTiled(float4 *__restrict__ newVel, float3 *__restrict__ forceOut,
-              const float4 *__restrict__ sortedPos, const float4 *__restrict__ sortedVel,
-              const unsigned *__restrict__ index, const unsigned *__restrict__ cellStart,
-              const unsigned *__restrict__ cellEnd, unsigned n, KParams kp,
-              float4 *__restrict__ posOut, unsigned *__restrict__ hashOut, float dt,
-              unsigned *status) {
+kCollideTiled(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
+              const float4 *__restrict__ sortedVel, const unsigned *__restrict__ index,
+              CellRanges cells, unsigned n, KParams kp, CollideOut out, unsigned *status) {
+  const unsigned *__restrict__ cellStart = cells.start;
+  const unsigned *__restrict__ cellEnd = cells.end;
   __shared__ TileSmem sm;
   __shared__ unsigned qj[kQueueLen * kQueueStride];
   __shared__ unsigned char qc[kQueueLen * kQueueStride];
@@ -472,9 +516,9 @@ kCollideTiled(float4 *__restrict__ newVel, float3 *__restrict__ forceOut,
                                     vel, ri, cdMono, cdMonoHi2, sortedVel, P, posOf, force);
         }
       } else {
-        force = neighbourForceGlobal<kRadiusFromW>(i, n, pos, vel, ri, g, false, sortedPos,
-                                                   sortedVel, cellStart, cellEnd, P,
-                                                   qj + tid, qc + tid);
+        force = neighbourForceGlobal<kRadiusFromW, false>(i, n, pos, vel, ri, g, false,
+                                                          sortedPos, sortedVel, cells, P,
+                                                          qj + tid, qc + tid);
       }
       done = true;
     }
@@ -482,28 +526,26 @@ kCollideTiled(float4 *__restrict__ newVel, float3 *__restrict__ forceOut,
     __syncthreads();  // the staged buffers are reused by the next group
   }
   if (valid && !done)  // particles past the last staged group
-    force = neighbourForceGlobal<kRadiusFromW>(i, n, pos, vel, ri, g, false, sortedPos,
-                                               sortedVel, cellStart, cellEnd, P, qj + tid,
-                                               qc + tid);
+    force = neighbourForceGlobal<kRadiusFromW, false>(i, n, pos, vel, ri, g, false, sortedPos,
+                                                      sortedVel, cells, P, qj + tid, qc + tid);
   if (valid)
     finishParticle<kMode, kCollider, kForceOut>(i, n, pos, vel, p4, ri, force, index, newVel,
-                                                forceOut, posOut, hashOut, dt, P);
+                                                out, P);
 }
 
-template <int kMode, bool kRadiusFromW, bool kCollider, bool kForceOut>
-void launchT(bool tiled, bool cull, unsigned n, float4 *newVel, float3 *force,
-             const float4 *sp, const float4 *sv, const unsigned *index, const unsigned *cs,
-             const unsigned *ce, const KParams &kp, float4 *posOut, unsigned *hashOut,
-             float dt) {
+template <int kMode, bool kRadiusFromW, bool kCollider, bool kForceOut, bool kPrefix>
+void launchT(bool tiled, bool cull, unsigned n, float4 *newVel, const float4 *sp,
+             const float4 *sv, const unsigned *index, const CellRanges &cells,
+             const KParams &kp, const CollideOut &out) {
   unsigned blocks = (n + 127) / 128;
-  if (tiled)
+  if (tiled && !kPrefix)
     kCollideTiled<kMode, kRadiusFromW, kCollider, kForceOut>
-        <<<blocks, kTileThreads, 0, curStream()>>>(newVel, force, sp, sv, index, cs, ce, n,
-                                                   kp, posOut, hashOut, dt, ctx().dStatus);
+        <<<blocks, kTileThreads, 0, curStream()>>>(newVel, sp, sv, index, cells, n, kp, out,
+                                                   ctx().dStatus);
   else
-    kCollideGlobal<kMode, kRadiusFromW, kCollider, kForceOut>
-        <<<blocks, 128, 0, curStream()>>>(newVel, force, sp, sv, index, cs, ce, n, kp,
-                                          posOut, hashOut, dt, cull, ctx().dStatus);
+    kCollideGlobal<kMode, kRadiusFromW, kCollider, kForceOut, kPrefix>
+        <<<blocks, 128, 0, curStream()>>>(newVel, sp, sv, index, cells, n, kp, out, cull,
+                                          ctx().dStatus);
 }
 
 int g_collidePath = -1;  // -1 auto, 0 global, 1 tiled (fcdemSetCollidePath)
@@ -511,14 +553,14 @@ bool g_cullCells = true;  // fcdemSetCellCulling
 
 }  // namespace
 
-void launchCollide(int mode, bool collider, float4 *newVel, float3 *force,
-                   const float4 *sp, const float4 *sv, const unsigned *index,
-                   const unsigned *cs, const unsigned *ce, unsigned n, const KParams &kp,
-                   float4 *posOut, unsigned *hashOut, float dt) {
+void launchCollide(int mode, bool collider, float4 *newVel, const float4 *sp,
+                   const float4 *sv, const unsigned *index, const CellRanges &cells,
+                   unsigned n, const KParams &kp, const CollideOut &out) {
   if (n == 0) return;
+  const bool prefix = cells.off != nullptr;
   // The bulk copies need 16-byte aligned positions; the tiled kernel is
   // opt-in (fcdemSetCollidePath(1)): the culled global kernel is faster.
-  bool tiled = g_collidePath == 1 && ((uintptr_t)sp & 15u) == 0;
+  bool tiled = !prefix && g_collidePath == 1 && ((uintptr_t)sp & 15u) == 0;
   // Culling is exact when every grid dimension is >= 3 and the largest
   // contact distance 2 * particleRadius fits in the smallest cell.
   const SimParams &P = kp.p;
@@ -527,24 +569,30 @@ void launchCollide(int mode, bool collider, float4 *newVel, float3 *force,
               P.gridSize[2] >= 3 && 2.0f * P.particleRadius <= minCell &&
               P.particleRadius > 0.0f;
   const bool w = kp.radiusFromW != 0;
-  const bool fo = force != nullptr;
-#define FCDEM_COLLIDE_CASE(M, W, C, F)                                                  \
-  if (mode == M && w == W && collider == C && fo == F) {                                \
-    launchT<M, W, C, F>(tiled, cull, n, newVel, force, sp, sv, index, cs, ce, kp,       \
-                        posOut, hashOut, dt);                                           \
-    launchOk();                                                                         \
-    return;                                                                             \
+  const bool fo = out.force != nullptr;
+#define FCDEM_COLLIDE_CASE(M, W, C, F, X)                                              \
+  if (mode == M && w == W && collider == C && fo == F && prefix == X) {                \
+    launchT<M, W, C, F, X>(tiled, cull, n, newVel, sp, sv, index, cells, kp, out);     \
+    launchOk();                                                                        \
+    return;                                                                            \
   }
-  FCDEM_COLLIDE_CASE(0, false, true, false)
-  FCDEM_COLLIDE_CASE(0, true, true, false)
-  FCDEM_COLLIDE_CASE(0, false, false, false)
-  FCDEM_COLLIDE_CASE(0, true, false, false)
-  FCDEM_COLLIDE_CASE(0, false, false, true)
-  FCDEM_COLLIDE_CASE(0, true, false, true)
-  FCDEM_COLLIDE_CASE(0, false, true, true)
-  FCDEM_COLLIDE_CASE(0, true, true, true)
-  FCDEM_COLLIDE_CASE(1, false, true, false)
-  FCDEM_COLLIDE_CASE(1, true, true, false)
+  // the reference-named stage (split cell tables)
+  FCDEM_COLLIDE_CASE(0, false, true, false, false)
+  FCDEM_COLLIDE_CASE(0, true, true, false, false)
+  FCDEM_COLLIDE_CASE(0, false, false, false, false)
+  FCDEM_COLLIDE_CASE(0, true, false, false, false)
+  FCDEM_COLLIDE_CASE(0, false, false, true, false)
+  FCDEM_COLLIDE_CASE(0, true, false, true, false)
+  FCDEM_COLLIDE_CASE(0, false, true, true, false)
+  FCDEM_COLLIDE_CASE(0, true, true, true, false)
+  // fcdemUpdate, radix-sort pipeline
+  FCDEM_COLLIDE_CASE(1, false, true, false, false)
+  FCDEM_COLLIDE_CASE(1, true, true, false, false)
+  // fcdemUpdate, counting-sort pipeline (prefix cell table)
+  FCDEM_COLLIDE_CASE(2, false, true, false, true)
+  FCDEM_COLLIDE_CASE(2, true, true, false, true)
+  FCDEM_COLLIDE_CASE(3, false, true, false, true)
+  FCDEM_COLLIDE_CASE(3, true, true, false, true)
 #undef FCDEM_COLLIDE_CASE
   setError(FCDEM_ERR_INVALID_VALUE);
 }

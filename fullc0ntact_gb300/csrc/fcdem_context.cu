@@ -227,6 +227,7 @@ int fcdemGetLastError(void) {
         if (status & kStatusTimeout) setError(FCDEM_ERR_DEVICE_TIMEOUT);
         else if (status & kStatusKeyRange) setError(FCDEM_ERR_KEY_RANGE);
         else if (status & kStatusRadiusBound) setError(FCDEM_ERR_RADIUS_BOUND);
+        else if (status & kStatusCellOverflow) setError(FCDEM_ERR_CELL_OVERFLOW);
       }
     } else {
       cudaGetLastError();
@@ -246,6 +247,8 @@ const char *fcdemGetErrorString(int code) {
     case FCDEM_ERR_DEVICE_TIMEOUT: return "a bounded device-side wait expired";
     case FCDEM_ERR_KEY_RANGE: return "sort key above the grid's key width";
     case FCDEM_ERR_ALLOC: return "device allocation failed";
+    case FCDEM_ERR_CELL_OVERFLOW:
+      return "fcdemUpdate: a cell holds more than 4096 particles (order inside it not stable)";
     case FCDEM_ERR_RADIUS_BOUND:
       return "radius-from-w mode: a particle radius exceeds SimParams.particleRadius";
     default: return "unknown error";

@@ -31,6 +31,7 @@ enum : unsigned {
   kStatusTimeout = 1u,   // a bounded spin-wait gave up
   kStatusKeyRange = 2u,  // a sort key had bits above the sorted width
   kStatusRadiusBound = 4u,  // radius-from-w mode: a radius above particleRadius
+  kStatusCellOverflow = 8u,  // counting sort: a cell too full for the stable fix-up
 };
 
 // Everything a kernel needs from the parameter block, passed by value so
@@ -50,6 +51,9 @@ struct Context {
   unsigned *dStatus = nullptr;  // one device word of kStatus* bits
   void *scratch = nullptr;      // grown on demand, never shrunk
   size_t scratchBytes = 0;
+  void *countBuf = nullptr;     // counting-sort pipeline of fcdemUpdate
+  size_t countBytes = 0;
+  unsigned countCells = 0;
 };
 
 // The context of the calling thread's current device (created on first use).
@@ -96,12 +100,48 @@ void radixSortPairs(Context &c, unsigned *keys, unsigned *vals, unsigned n,
 // Cell-table fill (cellStart = 0xffffffff).  Defined in fcdem_stages.cu.
 void fillU32(Context &c, unsigned *p, size_t count, unsigned value);
 
-// collide (particles_kernel.cu:185-293), defined in fcdem_collide.cu.
-// mode 0: newVel[index[i]] = (v + F, 0).  mode 1: also the next update's
-// integrate and calcHash (posOut, hashOut).  force != nullptr also stores F.
-void launchCollide(int mode, bool collider, float4 *newVel, float3 *force,
-                   const float4 *sp, const float4 *sv, const unsigned *index,
-                   const unsigned *cs, const unsigned *ce, unsigned n,
-                   const KParams &kp, float4 *posOut, unsigned *hashOut, float dt);
+// The cell ranges collide reads: either the reference's cellStart/cellEnd
+// pair (empty = 0xffffffff start), or a prefix table off[] over numCells + 1
+// cells (cell c = off[c] .. off[c+1]).
+struct CellRanges {
+  const unsigned *start = nullptr;
+  const unsigned *end = nullptr;
+  const unsigned *off = nullptr;
+};
+
+// What collide writes besides newVel (particles_kernel.cu:185-293 writes
+// only newVel[index[i]] = (v + F, 0)).
+struct CollideOut {
+  float3 *force = nullptr;     // F per particle (original order), optional
+  float4 *posOut = nullptr;    // mode 1/2: next-step integrated positions
+  unsigned *hashOut = nullptr; // mode 1/2: next-step cell hashes
+  unsigned *rankOut = nullptr; // mode 2: rank of the particle in its cell count
+  unsigned *cnt = nullptr;     // mode 2: per-cell counters (atomic)
+  float dt = 0.0f;
+};
+
+// collide, defined in fcdem_collide.cu.  mode 0: the reference's output.
+// mode 1: also the next update's integrate and calcHash.  mode 2 (counting
+// pipeline): the next update's integrate and calcHash, written at the
+// particle's sorted slot i (posOut[i], newVel[i], hashOut[i]) with its count
+// rank (rankOut[i]) -- the state stays in sorted order between fused steps.
+// mode 3 (last fused step): as 0, plus posOut[index[i]] = the position.
+void launchCollide(int mode, bool collider, float4 *newVel, const float4 *sp,
+                   const float4 *sv, const unsigned *index, const CellRanges &cells,
+                   unsigned n, const KParams &kp, const CollideOut &out);
+
+// The counting-sort pipeline of fcdemUpdate (fcdem_count.cu).
+struct CountBuffers {
+  unsigned *cnt, *off, *rank, *slotKey, *slotIdx, *slotPrev, *lookback;
+  unsigned scanTiles;
+};
+bool countPipelineBegin(Context &c, float4 *pos, float4 *vel, float dt, unsigned *hash,
+                        unsigned n, unsigned numCells, const KParams &kp, CountBuffers &b);
+bool countPipelineSort(Context &c, const CountBuffers &b, const unsigned *origOf,
+                       const float4 *prevPos, const float4 *prevVel, unsigned *hash,
+                       unsigned *index, float4 *sortedPos, float4 *sortedVel, unsigned n,
+                       unsigned numCells);
+bool countPipelineTables(const CountBuffers &b, unsigned *cellStart, unsigned *cellEnd,
+                         unsigned numCells);
 
 }  // namespace fcdem

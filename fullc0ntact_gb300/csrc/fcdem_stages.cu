@@ -156,6 +156,9 @@ static bool tablesOk(const SimParams &p, unsigned numCells) {
   return true;
 }
 
+// fcdemUpdate pipeline: 0 radix sort + reorder, 1 counting sort (default).
+int g_updatePipeline = 1;
+
 bool readyFor(const Context &c) {
   if (!c.haveParams) { setError(FCDEM_ERR_NO_PARAMS); return false; }
   if (!gridOk(c.params)) { setError(FCDEM_ERR_INVALID_VALUE); return false; }
@@ -225,9 +228,12 @@ void collide(float *newVel, float *sortedPos, float *sortedVel,
     setError(FCDEM_ERR_INVALID_VALUE);
     return;
   }
-  launchCollide(0, true, (float4 *)newVel, nullptr, (const float4 *)sortedPos,
-                (const float4 *)sortedVel, gridParticleIndex, cellStart,
-                cellEnd, numParticles, kparams(c), nullptr, nullptr, 0.0f);
+  CellRanges cells;
+  cells.start = cellStart;
+  cells.end = cellEnd;
+  launchCollide(0, true, (float4 *)newVel, (const float4 *)sortedPos,
+                (const float4 *)sortedVel, gridParticleIndex, cells, numParticles,
+                kparams(c), CollideOut());
 }
 
 void sortParticles(uint *dGridParticleHash, uint *dGridParticleIndex,
@@ -256,6 +262,49 @@ void fcdemUpdate(float *pos, float *vel, float *sortedPos, float *sortedVel,
   const KParams kp = kparams(c);
   const int bits = keyBits(c.params.numCells);
   const unsigned n = numParticles;
+  if (g_updatePipeline == 1) {
+    // Counting-sort pipeline (fcdem_count.cu).  Between fused steps the state
+    // stays in the previous step's sorted order: collide writes the
+    // integrated position/velocity, next hash and count rank of slot i at
+    // entry i of pos/vel/hash/rank, and the next scatter and fix-up read them
+    // in that order (near-sequential instead of random).  The first step
+    // starts from particle order; the last collide writes vel and pos back in
+    // particle order, and the cell tables are written once at the end.
+    CountBuffers b;
+    stageBegin(0);
+    bool ok = countPipelineBegin(c, (float4 *)pos, (float4 *)vel, deltaTime, hash, n,
+                                 numCells, kp, b);
+    stageEnd(0);
+    for (uint s = 0; ok && s < steps; ++s) {
+      stageBegin(1);
+      ok = countPipelineSort(c, b, s == 0 ? nullptr : index, (const float4 *)pos,
+                             (const float4 *)vel, hash, index, (float4 *)sortedPos,
+                             (float4 *)sortedVel, n, numCells);
+      stageEnd(1);
+      if (!ok) break;
+      const bool last = (s + 1 == steps);
+      CellRanges cells;
+      cells.off = b.off;
+      CollideOut out;
+      out.posOut = (float4 *)pos;
+      if (!last) {
+        out.hashOut = hash;
+        out.rankOut = b.rank;
+        out.cnt = b.cnt;
+        out.dt = deltaTime;
+      }
+      stageBegin(4);
+      launchCollide(last ? 3 : 2, true, (float4 *)vel, (const float4 *)sortedPos,
+                    (const float4 *)sortedVel, index, cells, n, kp, out);
+      stageEnd(4);
+    }
+    if (ok) {
+      stageBegin(2);
+      countPipelineTables(b, cellStart, cellEnd, numCells);
+      stageEnd(2);
+    }
+    return;
+  }
   stageBegin(0);
   launchIntegrateHash((float4 *)pos, (float4 *)vel, deltaTime, hash, index, n, kp);
   stageEnd(0);
@@ -273,12 +322,22 @@ void fcdemUpdate(float *pos, float *vel, float *sortedPos, float *sortedVel,
                   hash, index, (const float4 *)pos, (const float4 *)vel, n, numCells);
     stageEnd(3);
     const bool last = (s + 1 == steps);
+    CellRanges cells;
+    cells.start = cellStart;
+    cells.end = cellEnd;
+    CollideOut out;
+    if (!last) {
+      out.posOut = (float4 *)pos;
+      out.hashOut = hash;
+      out.dt = deltaTime;
+    }
     stageBegin(4);
-    launchCollide(last ? 0 : 1, true, (float4 *)vel, nullptr,
-                  (const float4 *)sortedPos, (const float4 *)sortedVel, index,
-                  cellStart, cellEnd, n, kp, (float4 *)pos, hash, deltaTime);
+    launchCollide(last ? 0 : 1, true, (float4 *)vel, (const float4 *)sortedPos,
+                  (const float4 *)sortedVel, index, cells, n, kp, out);
     stageEnd(4);
   }
 }
+
+void fcdemSetUpdatePipeline(int pipeline) { g_updatePipeline = pipeline == 0 ? 0 : 1; }
 
 }  // extern "C"

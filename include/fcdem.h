@@ -153,6 +153,7 @@ void collide(float *newVel, float *sortedPos, float *sortedVel,
 #define FCDEM_ERR_KEY_RANGE         6  /* sort key above the grid's key width */
 #define FCDEM_ERR_ALLOC             7  /* device scratch allocation failed    */
 #define FCDEM_ERR_RADIUS_BOUND      8  /* a radius above particleRadius (w mode) */
+#define FCDEM_ERR_CELL_OVERFLOW     9  /* fcdemUpdate: > 4096 particles in a cell */
 
 /* Returns and clears the first error recorded since the last call.  It
  * synchronises the library stream so that device-side status words (bounded
@@ -196,6 +197,16 @@ void fcdemUpdate(float *pos, float *vel, float *sortedPos, float *sortedVel,
  * kernel, 1 the shared-memory tiled kernel.  Both give identical results. */
 void fcdemSetCollidePath(int path);
 
+/* Sort tuning.  The counting passes of the sort come in several block
+ * shapes (threads x keys per thread); results are identical.
+ * fcdemAutotuneSort times each on numParticles uniform keys below numCells
+ * (allocating temporary device memory), keeps the fastest for that size
+ * class (power-of-two bucket of numParticles) and returns its index (-1 on
+ * error); *bestMs receives its time.  fcdemSetSortConfig forces one
+ * (-1 = default) and returns the number of configurations. */
+int fcdemAutotuneSort(unsigned numParticles, unsigned numCells, float *bestMs);
+int fcdemSetSortConfig(unsigned numParticles, int config);
+
 /* Number of kernels this library has launched in this process. */
 unsigned long long fcdemGetLaunchCount(void);
 
@@ -209,6 +220,11 @@ unsigned long long fcdemGetLaunchCount(void);
 #define FCDEM_NUM_STAGES 5
 void fcdemSetProfiling(int on);
 int fcdemGetStageTimes(float *ms, unsigned *launches, int maxStages);
+
+/* fcdemUpdate's sort: 1 (default) a counting sort over the cells with a
+ * stable within-cell fix-up fused with the reorder gather; 0 the radix sort,
+ * cell-table fill and reorder of the stage functions.  Results are identical. */
+void fcdemSetUpdatePipeline(int pipeline);
 
 /* ---------------------------------------------------------------------- */
 /* Scene generators (host memory, 4 floats per particle).  Deterministic for

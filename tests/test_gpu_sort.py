@@ -79,3 +79,38 @@ def test_repeated_sorts_reuse_scratch():
         k, v = _sort_gpu(keys, vals, 2 ** 24)
         rk, rv = _sort_cpu(keys, vals)
         np.testing.assert_array_equal(v, rv)
+
+
+@pytest.mark.parametrize("n", [5000, 300_001])
+def test_every_pass_configuration_sorts_identically(n):
+    from fullc0ntact_gb300 import dem
+    lib = dem.lib
+    count = lib.fcdemSetSortConfig(n, -1)
+    assert count >= 2
+    rng = np.random.default_rng(n + 1)
+    keys = rng.integers(0, 2 ** 24, n).astype(np.uint32)
+    vals = np.arange(n, dtype=np.uint32)
+    rk, rv = _sort_cpu(keys, vals)
+    try:
+        for k in range(count):
+            assert lib.fcdemSetSortConfig(n, k) == count
+            gk, gv = _sort_gpu(keys, vals, 2 ** 24)
+            np.testing.assert_array_equal(gk, rk)
+            np.testing.assert_array_equal(gv, rv)
+    finally:
+        lib.fcdemSetSortConfig(n, -1)
+
+
+def test_autotune_picks_a_configuration():
+    import ctypes as C
+    from fullc0ntact_gb300 import dem
+    t = C.c_float()
+    best = dem.lib.fcdemAutotuneSort(200_000, 2 ** 24, C.byref(t))
+    dem.check("autotune")
+    assert best >= 0 and t.value > 0.0
+    keys = np.random.default_rng(3).integers(0, 2 ** 24, 200_000).astype(np.uint32)
+    vals = np.arange(200_000, dtype=np.uint32)
+    gk, gv = _sort_gpu(keys, vals, 2 ** 24)
+    rk, rv = _sort_cpu(keys, vals)
+    np.testing.assert_array_equal(gv, rv)
+    dem.lib.fcdemSetSortConfig(200_000, -1)

@@ -16,16 +16,23 @@ def _state(ds):
             ds.sorted_pos.cpu().numpy().copy(), ds.sorted_vel.cpu().numpy().copy())
 
 
+@pytest.mark.parametrize("pipeline", [0, 1])
 @pytest.mark.parametrize("poly", [False, True])
 @pytest.mark.parametrize("steps", [1, 2, 5])
-def test_fused_update_equals_staged(poly, steps):
+def test_fused_update_equals_staged(pipeline, poly, steps):
+    """Both fcdemUpdate pipelines (0: radix sort + fill + reorder, 1: cell
+    counting sort with stable fix-up) against the five staged calls."""
     from fullc0ntact_gb300 import dem, scenes
     sc = (scenes.random_box(5000, grid=(32, 32, 32), radius=1.0 / 24.0, seed=3, poly=True)
           if poly else scenes.config0(4096))
     a, b = dem.DeviceScene(sc), dem.DeviceScene(sc)
     for _ in range(steps):
         a.stages()
-    b.update(steps)
+    dem.lib.fcdemSetUpdatePipeline(pipeline)
+    try:
+        b.update(steps)
+    finally:
+        dem.lib.fcdemSetUpdatePipeline(1)
     dem.check("update")
     for x, y in zip(_state(a), _state(b)):
         np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
@@ -112,3 +119,19 @@ def test_stream_selection():
     s.synchronize()
     dem.check()
     np.testing.assert_array_equal(a.vel.cpu().numpy(), b.vel.cpu().numpy())
+
+
+def test_counting_pipeline_on_packed_scene_and_crowded_cells():
+    """The counting sort's within-cell fix-up on a scene with crowded cells
+    (40 particles in one cell) and on a packed polydisperse scene."""
+    from fullc0ntact_gb300 import dem, scenes
+    for sc in (scenes.random_box(3000, grid=(8, 8, 8), radius=0.02, cell=0.25, seed=4),
+               scenes.config1(100_000, grid=128)):
+        sc["pos"][:40, :3] = 0.01 + 0.001 * np.arange(40, dtype=np.float32)[:, None]
+        a, b = dem.DeviceScene(sc), dem.DeviceScene(sc)
+        for _ in range(3):
+            a.stages()
+        b.update(3)
+        dem.check("update")
+        for x, y in zip(_state(a), _state(b)):
+            np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
