@@ -94,6 +94,7 @@ __device__ __forceinline__ void finishParticle(
     const unsigned h = gridHash(gn.x, gn.y, gn.z, P);
     out.hashOut[i] = h;
     out.rankOut[i] = atomicAdd(out.cnt + h, 1u);
+    countTile(out.tileCnt, h >> 12);  // per 4096-cell tile (the scan's)
     return;
   }
   unsigned o = __ldg(index + i);

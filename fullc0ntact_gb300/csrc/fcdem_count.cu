@@ -7,10 +7,14 @@
 //
 //   count   the kernel that computes a particle's cell hash h (the fused
 //           collide+integrate of the previous step, or kIntegrateHashCount)
-//           also takes r = atomicAdd(&cnt[h], 1);
-//   scan    kScanCells: off = exclusive prefix sum of cnt over C + 1 cells
-//           (single pass, decoupled look-back), and cnt is cleared for the
-//           next step; off[c] .. off[c+1] is cell c's range, empty or not;
+//           also takes r = atomicAdd(&cnt[h], 1) and counts h's 4096-cell
+//           tile in tileCnt;
+//   scan    kScanTiles (one CTA) scans the tile counts, kScanCells scans
+//           each tile's cells from its tile offset -- no inter-CTA waits; a
+//           tile without particles writes its constant offsets and skips
+//           reading cnt.  off = exclusive prefix sum of cnt over C + 1 cells,
+//           cnt and tileCnt are cleared for the next step; off[c] .. off[c+1]
+//           is cell c's range, empty or not;
 //   scatter kScatterCells: slot off[h] + r receives (h, particle);
 //   fix-up  kFixupGather: the atomic ranks order a cell's members
 //           arbitrarily, so each slot re-ranks its particle among the
@@ -31,130 +35,138 @@ namespace {
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;
 constexpr int kScanTile = kScanThreads * kScanItems;  // 4096 cells
-constexpr unsigned kFlagAgg = 1u << 30;
-constexpr unsigned kFlagPrefix = 2u << 30;
-constexpr unsigned kValueMask = (1u << 30) - 1u;
-constexpr unsigned kSpinLimit = 1u << 22;
+constexpr int kTileShift = 12;  // log2(kScanTile)
 constexpr unsigned kEmpty = 0xffffffffu;
+static_assert((1 << kTileShift) == kScanTile, "tile shift");
 
-__device__ __forceinline__ unsigned ldVolatile(const unsigned *p) {
-  return *(const volatile unsigned *)p;
-}
-__device__ __forceinline__ void stVolatile(unsigned *p, unsigned v) {
-  *(volatile unsigned *)p = v;
+// Exclusive prefix sums of the per-tile counts (one tile = kScanTile cells):
+// tileOff[t] = sum of tileCnt[0..t), tileOff[tiles] = the total; tileCnt is
+// cleared for the next step.  One CTA of 1024 threads, tiles in chunks.
+__global__ void __launch_bounds__(1024)
+kScanTiles(unsigned *__restrict__ tileCnt, unsigned *__restrict__ tileOff, unsigned tiles) {
+  __shared__ unsigned sWarp[32];
+  __shared__ unsigned sCarry;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) sCarry = 0;
+  __syncthreads();
+  for (unsigned base = 0; base < tiles; base += 1024) {
+    const unsigned t = base + tid;
+    const unsigned v = t < tiles ? tileCnt[t] : 0u;
+    unsigned x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) sWarp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      unsigned w = sWarp[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        unsigned y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      sWarp[lane] = w;
+    }
+    __syncthreads();
+    const unsigned carry = sCarry;
+    if (t < tiles) {
+      tileOff[t] = carry + (warp ? sWarp[warp - 1] : 0u) + x - v;
+      tileCnt[t] = 0u;
+    }
+    __syncthreads();
+    if (tid == 0) sCarry = carry + sWarp[31];
+    __syncthreads();
+  }
+  if (tid == 0) tileOff[tiles] = sCarry;
 }
 
-// Exclusive prefix sum of cnt[0..m) into off[0..m), clearing cnt.  lookback
-// (one word per tile) and *tileCounter must be zero on entry.
+// off[c] = tileOff[tile] + exclusive prefix of cnt within the tile, cnt
+// cleared.  A tile without particles only writes its constant offsets.
+// Round q of a tile covers cells q*1024 .. +1024, thread t the four at 4t
+// (16-byte accesses, coalesced).
 __global__ void __launch_bounds__(kScanThreads)
 kScanCells(unsigned *__restrict__ cnt, unsigned *__restrict__ off, unsigned m,
-           unsigned *lookback, unsigned *tileCounter, unsigned *status) {
-  __shared__ unsigned sTile, sExcl;
+           const unsigned *__restrict__ tileOff) {
   __shared__ unsigned sWarp[kScanThreads / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) sTile = atomicAdd(tileCounter, 1u);
-  __syncthreads();
-  const unsigned tile = sTile;
-  const size_t base = (size_t)tile * kScanTile + (size_t)tid * kScanItems;
-  unsigned v[kScanItems];
-  unsigned sum = 0;
-  // a thread owns kScanItems consecutive cells (16-byte loads when whole)
-  if (base + kScanItems <= m && ((base & 3u) == 0)) {
+  const unsigned tile = blockIdx.x;
+  constexpr int kRounds = kScanItems / 4;
+  const size_t tbase = (size_t)tile * kScanTile;
+  const unsigned t0 = __ldg(tileOff + tile), t1 = __ldg(tileOff + tile + 1);
+  if (t0 == t1) {  // empty tile: every cell starts (and ends) at t0
 #pragma unroll
-    for (int q = 0; q < kScanItems / 4; ++q) {
-      uint4 t = reinterpret_cast<const uint4 *>(cnt + base)[q];
-      v[4 * q] = t.x; v[4 * q + 1] = t.y; v[4 * q + 2] = t.z; v[4 * q + 3] = t.w;
+    for (int q = 0; q < kRounds; ++q) {
+      const size_t c0 = tbase + (size_t)q * (kScanThreads * 4) + (size_t)tid * 4;
+      if (c0 + 4 <= m) {
+        reinterpret_cast<uint4 *>(off + c0)[0] = make_uint4(t0, t0, t0, t0);
+      } else {
+        for (int k = 0; k < 4; ++k)
+          if (c0 + k < m) off[c0 + k] = t0;
+      }
     }
-  } else {
-#pragma unroll
-    for (int q = 0; q < kScanItems; ++q) v[q] = base + q < m ? cnt[base + q] : 0u;
+    return;
   }
+  uint4 v[kRounds];
+  unsigned excl[kRounds];
 #pragma unroll
-  for (int q = 0; q < kScanItems; ++q) sum += v[q];
-  // block exclusive scan of the per-thread sums
-  unsigned x = sum;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    unsigned y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) sWarp[warp] = x;
-  __syncthreads();
-  if (warp == 0) {
-    unsigned s = lane < kScanThreads / 32 ? sWarp[lane] : 0u;
-#pragma unroll
-    for (int o = 1; o < kScanThreads / 32; o <<= 1) {
-      unsigned y = __shfl_up_sync(0xffffffffu, s, o);
-      if (lane >= o) s += y;
-    }
-    if (lane < kScanThreads / 32) sWarp[lane] = s;
-  }
-  __syncthreads();
-  const unsigned threadExcl = (warp ? sWarp[warp - 1] : 0u) + x - sum;
-  const unsigned tileSum = sWarp[kScanThreads / 32 - 1];
-  // decoupled look-back for the tile's exclusive prefix, warp 0 reading 32
-  // predecessor tiles per round
-  if (warp == 0) {
-    unsigned excl = 0;
-    if (tile == 0) {
-      if (lane == 0) stVolatile(lookback, kFlagPrefix | (tileSum & kValueMask));
+  for (int q = 0; q < kRounds; ++q) {  // all loads in flight before the scans
+    const size_t c0 = tbase + (size_t)q * (kScanThreads * 4) + (size_t)tid * 4;
+    if (c0 + 4 <= m) {
+      v[q] = reinterpret_cast<const uint4 *>(cnt + c0)[0];
     } else {
-      if (lane == 0) stVolatile(lookback + tile, kFlagAgg | (tileSum & kValueMask));
-      int t = (int)tile - 1;  // newest tile of this round (lane 0)
-      unsigned spins = 0;
-      while (t >= 0) {
-        const int mine = t - lane;
-        unsigned w = mine >= 0 ? ldVolatile(lookback + mine) : (kFlagPrefix | 0u);
-        unsigned flag = w & ~kValueMask;
-        // wait while a tile before the closest inclusive prefix has not
-        // published anything yet
-        const unsigned preMask = __ballot_sync(0xffffffffu, flag == kFlagPrefix);
-        const unsigned zeroMask = __ballot_sync(0xffffffffu, flag == 0u);
-        const unsigned relevant = preMask ? ((preMask & (0u - preMask)) - 1u) : 0xffffffffu;
-        if (zeroMask & relevant) {
-          if (++spins > kSpinLimit) {
-            if (lane == 0) atomicOr(status, (unsigned)kStatusTimeout);
-            break;
-          }
-          if (spins > 64) __nanosleep(64);
-          continue;
+      v[q].x = c0 < m ? cnt[c0] : 0u;
+      v[q].y = c0 + 1 < m ? cnt[c0 + 1] : 0u;
+      v[q].z = c0 + 2 < m ? cnt[c0 + 2] : 0u;
+      v[q].w = c0 + 3 < m ? cnt[c0 + 3] : 0u;
+    }
+  }
+  unsigned carry = 0;
+#pragma unroll
+  for (int q = 0; q < kRounds; ++q) {
+    const unsigned sum = v[q].x + v[q].y + v[q].z + v[q].w;
+    unsigned x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) sWarp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      unsigned w = lane < kScanThreads / 32 ? sWarp[lane] : 0u;
+#pragma unroll
+      for (int o = 1; o < kScanThreads / 32; o <<= 1) {
+        unsigned y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      if (lane < kScanThreads / 32) sWarp[lane] = w;
+    }
+    __syncthreads();
+    excl[q] = carry + (warp ? sWarp[warp - 1] : 0u) + x - sum;
+    carry += sWarp[kScanThreads / 32 - 1];
+    __syncthreads();  // sWarp is reused by the next round
+  }
+#pragma unroll
+  for (int q = 0; q < kRounds; ++q) {
+    const size_t c0 = tbase + (size_t)q * (kScanThreads * 4) + (size_t)tid * 4;
+    uint4 o;
+    o.x = t0 + excl[q];
+    o.y = o.x + v[q].x;
+    o.z = o.y + v[q].y;
+    o.w = o.z + v[q].z;
+    if (c0 + 4 <= m) {
+      reinterpret_cast<uint4 *>(off + c0)[0] = o;
+      reinterpret_cast<uint4 *>(cnt + c0)[0] = make_uint4(0u, 0u, 0u, 0u);
+    } else {
+      const unsigned ov[4] = {o.x, o.y, o.z, o.w};
+      for (int k = 0; k < 4; ++k)
+        if (c0 + k < m) {
+          off[c0 + k] = ov[k];
+          cnt[c0 + k] = 0u;
         }
-        // the closest lane holding an inclusive prefix ends the walk
-        unsigned pre = __ballot_sync(0xffffffffu, flag == kFlagPrefix);
-        int stop = pre ? __ffs(pre) - 1 : 31;
-        unsigned v = lane <= stop ? (w & kValueMask) : 0u;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        excl += v;
-        if (pre) break;
-        t -= 32;
-      }
-      if (lane == 0) stVolatile(lookback + tile, kFlagPrefix | ((excl + tileSum) & kValueMask));
     }
-    if (lane == 0) sExcl = excl;
-  }
-  __syncthreads();
-  unsigned run = sExcl + threadExcl;
-  unsigned o[kScanItems];
-#pragma unroll
-  for (int q = 0; q < kScanItems; ++q) {
-    o[q] = run;
-    run += v[q];
-  }
-  if (base + kScanItems <= m && ((base & 3u) == 0)) {
-#pragma unroll
-    for (int q = 0; q < kScanItems / 4; ++q) {
-      reinterpret_cast<uint4 *>(off + base)[q] = make_uint4(o[4 * q], o[4 * q + 1],
-                                                            o[4 * q + 2], o[4 * q + 3]);
-      reinterpret_cast<uint4 *>(cnt + base)[q] = make_uint4(0u, 0u, 0u, 0u);
-    }
-  } else {
-#pragma unroll
-    for (int q = 0; q < kScanItems; ++q)
-      if (base + q < m) {
-        off[base + q] = o[q];
-        cnt[base + q] = 0u;
-      }
   }
 }
 
@@ -235,7 +247,8 @@ kCellTables(const unsigned *__restrict__ off, unsigned *__restrict__ cellStart,
   }
 }
 
-// First step of fcdemUpdate: integrate + calcHash + count.
+// First step of fcdemUpdate: integrate + calcHash + count (the tile counts
+// follow in kTileReduce).
 __global__ void __launch_bounds__(256)
 kIntegrateHashCount(float4 *__restrict__ pos, float4 *__restrict__ vel, float dt,
                     unsigned *__restrict__ hash, unsigned *__restrict__ rank,
@@ -254,6 +267,37 @@ kIntegrateHashCount(float4 *__restrict__ pos, float4 *__restrict__ vel, float dt
   rank[i] = atomicAdd(cnt + h, 1u);
 }
 
+// tileCnt[t] = sum of cnt over tile t (after kIntegrateHashCount, whose
+// particle-order cells are scattered over the tiles: summing the counts once
+// is cheaper than one atomic per particle on the few tile counters).
+__global__ void __launch_bounds__(kScanThreads)
+kTileReduce(const unsigned *__restrict__ cnt, unsigned *__restrict__ tileCnt, unsigned m) {
+  __shared__ unsigned sWarp[kScanThreads / 32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const size_t tbase = (size_t)blockIdx.x * kScanTile;
+  unsigned sum = 0;
+#pragma unroll
+  for (int q = 0; q < kScanItems / 4; ++q) {
+    const size_t c0 = tbase + (size_t)q * (kScanThreads * 4) + (size_t)tid * 4;
+    if (c0 + 4 <= m) {
+      uint4 v = reinterpret_cast<const uint4 *>(cnt + c0)[0];
+      sum += v.x + v.y + v.z + v.w;
+    } else {
+      for (int k = 0; k < 4; ++k)
+        if (c0 + k < m) sum += cnt[c0 + k];
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if (lane == 0) sWarp[warp] = sum;
+  __syncthreads();
+  if (tid == 0) {
+    unsigned t = 0;
+    for (int w = 0; w < kScanThreads / 32; ++w) t += sWarp[w];
+    tileCnt[blockIdx.x] = t;
+  }
+}
+
 }  // namespace
 
 // Buffers of the pipeline, kept in the context between calls: cnt (all zero
@@ -263,7 +307,7 @@ static bool countBuffers(Context &c, unsigned n, unsigned numCells, CountBuffers
   const size_t m = (size_t)numCells + 1;
   const unsigned tiles = (unsigned)((m + kScanTile - 1) / kScanTile);
   auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
-  const size_t need = 2 * al(m * 4) + 4 * al((size_t)n * 4) + al((size_t)(tiles + 1) * 4);
+  const size_t need = 2 * al(m * 4) + 4 * al((size_t)n * 4) + 2 * al((size_t)(tiles + 1) * 4);
   if (c.countBuf == nullptr || c.countBytes < need || c.countCells != numCells) {
     if (!cudaOk(cudaDeviceSynchronize())) return false;
     if (c.countBuf) cudaFree(c.countBuf);
@@ -279,11 +323,18 @@ static bool countBuffers(Context &c, unsigned n, unsigned numCells, CountBuffers
     c.countCells = numCells;
     if (!cudaOk(cudaMemset(c.countBuf, 0, need))) return false;  // cnt starts at zero
   }
+  // The arrays that must stay zero between calls (cnt, tileCnt) sit first,
+  // at offsets that depend on the cell count only, so that a call with
+  // another particle count reuses them in place.
   char *p = (char *)c.countBuf;
   b.cnt = (unsigned *)p;
   p += al(m * 4);
+  b.tileCnt = (unsigned *)p;
+  p += al((size_t)(tiles + 1) * 4);
   b.off = (unsigned *)p;
   p += al(m * 4);
+  b.tileOff = (unsigned *)p;
+  p += al((size_t)(tiles + 1) * 4);
   b.rank = (unsigned *)p;
   p += al((size_t)n * 4);
   b.slotKey = (unsigned *)p;
@@ -291,8 +342,6 @@ static bool countBuffers(Context &c, unsigned n, unsigned numCells, CountBuffers
   b.slotIdx = (unsigned *)p;
   p += al((size_t)n * 4);
   b.slotPrev = (unsigned *)p;
-  p += al((size_t)n * 4);
-  b.lookback = (unsigned *)p;
   b.scanTiles = tiles;
   return true;
 }
@@ -302,6 +351,8 @@ bool countPipelineBegin(Context &c, float4 *pos, float4 *vel, float dt, unsigned
   if (!countBuffers(c, n, numCells, b)) return false;
   kIntegrateHashCount<<<(n + 255) / 256, 256, 0, curStream()>>>(pos, vel, dt, hash, b.rank,
                                                                 b.cnt, n, kp);
+  if (!launchOk()) return false;
+  kTileReduce<<<b.scanTiles, kScanThreads, 0, curStream()>>>(b.cnt, b.tileCnt, numCells + 1);
   return launchOk();
 }
 
@@ -314,9 +365,9 @@ bool countPipelineSort(Context &c, const CountBuffers &b, const unsigned *origOf
                        unsigned numCells) {
   cudaStream_t st = curStream();
   const unsigned m = numCells + 1;
-  if (!cudaOk(cudaMemsetAsync(b.lookback, 0, (size_t)(b.scanTiles + 1) * 4, st))) return false;
-  kScanCells<<<b.scanTiles, kScanThreads, 0, st>>>(b.cnt, b.off, m, b.lookback,
-                                                   b.lookback + b.scanTiles, c.dStatus);
+  kScanTiles<<<1, 1024, 0, st>>>(b.tileCnt, b.tileOff, b.scanTiles);
+  if (!launchOk()) return false;
+  kScanCells<<<b.scanTiles, kScanThreads, 0, st>>>(b.cnt, b.off, m, b.tileOff);
   if (!launchOk()) return false;
   // hash holds the new hashes in entry order until the fix-up overwrites it
   kScatterCells<<<(n + 255) / 256, 256, 0, st>>>(hash, b.rank, origOf, b.off, b.slotKey,

@@ -99,4 +99,15 @@ __device__ __forceinline__ float rejectBound(float cd) {
   return (cd * cd) * 1.0000025f;
 }
 
+// tileCnt[tile] += 1 for every calling lane, one atomic per distinct tile in
+// the warp (consecutive sorted particles share tiles, so the atomics would
+// otherwise queue on a few addresses).  Call from converged code or with the
+// lanes that count.
+__device__ __forceinline__ void countTile(unsigned *tileCnt, unsigned tile) {
+  const unsigned active = __activemask();
+  const unsigned peers = __match_any_sync(active, tile);
+  const unsigned lane = threadIdx.x & 31u;
+  if ((peers & ((1u << lane) - 1u)) == 0u) atomicAdd(tileCnt + tile, (unsigned)__popc(peers));
+}
+
 }  // namespace fcdem

@@ -117,6 +117,7 @@ struct CollideOut {
   unsigned *hashOut = nullptr; // mode 1/2: next-step cell hashes
   unsigned *rankOut = nullptr; // mode 2: rank of the particle in its cell count
   unsigned *cnt = nullptr;     // mode 2: per-cell counters (atomic)
+  unsigned *tileCnt = nullptr; // mode 2: per-4096-cell-tile counters (atomic)
   float dt = 0.0f;
 };
 
@@ -132,7 +133,8 @@ void launchCollide(int mode, bool collider, float4 *newVel, const float4 *sp,
 
 // The counting-sort pipeline of fcdemUpdate (fcdem_count.cu).
 struct CountBuffers {
-  unsigned *cnt, *off, *rank, *slotKey, *slotIdx, *slotPrev, *lookback;
+  unsigned *cnt, *off, *rank, *slotKey, *slotIdx, *slotPrev;
+  unsigned *tileCnt, *tileOff;  // per 4096-cell tile: counts and their prefix
   unsigned scanTiles;
 };
 bool countPipelineBegin(Context &c, float4 *pos, float4 *vel, float dt, unsigned *hash,

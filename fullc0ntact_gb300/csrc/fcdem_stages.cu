@@ -291,6 +291,7 @@ void fcdemUpdate(float *pos, float *vel, float *sortedPos, float *sortedVel,
         out.hashOut = hash;
         out.rankOut = b.rank;
         out.cnt = b.cnt;
+        out.tileCnt = b.tileCnt;
         out.dt = deltaTime;
       }
       stageBegin(4);
