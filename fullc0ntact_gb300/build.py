@@ -21,6 +21,7 @@ SOURCES = [
     "fcdem_sort.cu",
     "fcdem_collide.cu",
     "fcdem_count.cu",
+    "fcdem_distmap.cu",
     "fcdem_host.cpp",
 ]
 

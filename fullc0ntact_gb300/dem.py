@@ -203,3 +203,99 @@ class ParticleSystem:
 
     def set_radius_from_w(self, on: bool) -> None:
         lib.fcdemPS_setRadiusFromW(self._h, int(on))
+
+
+# --- distance maps and the particledem_um entry points ----------------------
+
+_DM_SIGS = {
+    "fcdemDistMapCreate": (C.c_void_p, [C.c_void_p, C.c_void_p, C.POINTER(C.c_float),
+                                        C.POINTER(C.c_float), C.c_float, C.POINTER(C.c_int)]),
+    "fcdemDistMapTorus": (C.c_void_p, [C.c_float, C.c_float, C.c_int, C.c_float]),
+    "fcdemDistMapDestroy": (None, [C.c_void_p]),
+    "fcdemDistMapGeometry": (None, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                    C.POINTER(C.c_float), C.POINTER(C.c_int)]),
+    "fcdemDistMapVertices": (None, [C.c_void_p, C.c_void_p]),
+    "fcdemDistMapQuery": (None, [C.c_void_p, C.c_void_p, C.c_uint, C.c_void_p, C.c_void_p]),
+    "fcdemUM_integrateSystem": (None, [C.c_void_p, C.c_void_p, C.c_float, C.c_uint,
+                                       C.c_void_p]),
+    "fcdemUM_evalForces": (None, [C.c_void_p] * 7 + [C.c_uint, C.c_uint]),
+    "fcdemUM_reorderDataAndFindCellStart": (None, [C.c_void_p] * 8 + [C.c_uint, C.c_uint]),
+}
+for _n, (_r, _a) in _DM_SIGS.items():
+    getattr(lib, _n).restype = _r
+    getattr(lib, _n).argtypes = _a
+
+
+def _f3(v):
+    return (C.c_float * 3)(*[float(x) for x in v])
+
+
+class DistanceMap:
+    """A distance map on the device (DistanceMap<float,gpu>,
+    cuda_addon/distancemap.cuh:6-116)."""
+
+    def __init__(self, handle):
+        if not handle:
+            raise MemoryError("distance map creation failed")
+        self._h = handle
+        vmin, vmax = (C.c_float * 3)(), (C.c_float * 3)()
+        cs, cells = C.c_float(), (C.c_int * 3)()
+        lib.fcdemDistMapGeometry(handle, vmin, vmax, C.byref(cs), cells)
+        self.vmin, self.vmax = np.array(vmin, np.float32), np.array(vmax, np.float32)
+        self.cell_size, self.cells = cs.value, np.array(cells, np.int32)
+
+    @classmethod
+    def from_arrays(cls, distance, contact_points, vmin, vmax, cell_size, cells):
+        d = np.ascontiguousarray(distance, np.float32)
+        c = np.ascontiguousarray(contact_points, np.float32)
+        h = lib.fcdemDistMapCreate(d.ctypes.data, c.ctypes.data, _f3(vmin), _f3(vmax),
+                                   float(cell_size), (C.c_int * 3)(*[int(x) for x in cells]))
+        check("fcdemDistMapCreate")
+        return cls(h)
+
+    @classmethod
+    def torus(cls, major_radius=0.3, tube_radius=0.1, cells_per_axis=128, margin=0.05):
+        h = lib.fcdemDistMapTorus(major_radius, tube_radius, cells_per_axis, margin)
+        check("fcdemDistMapTorus")
+        return cls(h)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def vertices(self) -> np.ndarray:
+        nv = int(np.prod(self.cells + 1))
+        out = np.zeros((nv, 4), np.float32)
+        lib.fcdemDistMapVertices(self._h, out.ctypes.data)
+        check("fcdemDistMapVertices")
+        return out
+
+    def query(self, q: torch.Tensor):
+        n = q.shape[0]
+        dist = torch.empty(n, dtype=torch.float32, device=q.device)
+        cp = torch.empty((n, 4), dtype=torch.float32, device=q.device)
+        lib.fcdemDistMapQuery(self._h, _p(q), n, _p(dist), _p(cp))
+        return dist, cp
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib.fcdemDistMapDestroy(h)
+            self._h = None
+
+
+def um_integrate_system(pos, vel, dt: float, n: int, dmap: DistanceMap | None) -> None:
+    lib.fcdemUM_integrateSystem(_p(pos), _p(vel), dt, n, dmap.handle if dmap else None)
+
+
+def um_eval_forces(new_vel, force, sorted_pos, sorted_vel, index, cell_start, cell_end,
+                   n: int, num_cells: int) -> None:
+    lib.fcdemUM_evalForces(_p(new_vel), _p(force), _p(sorted_pos), _p(sorted_vel), _p(index),
+                           _p(cell_start), _p(cell_end), n, num_cells)
+
+
+def um_reorder(cell_start, cell_end, sorted_pos, sorted_vel, hash_, index, old_pos, old_vel,
+               n: int, num_cells: int) -> None:
+    lib.fcdemUM_reorderDataAndFindCellStart(_p(cell_start), _p(cell_end), _p(sorted_pos),
+                                            _p(sorted_vel), _p(hash_), _p(index), _p(old_pos),
+                                            _p(old_vel), n, num_cells)

@@ -227,6 +227,59 @@ int fcdemGetStageTimes(float *ms, unsigned *launches, int maxStages);
 void fcdemSetUpdatePipeline(int pipeline);
 
 /* ---------------------------------------------------------------------- */
+/* Distance maps (inshape3dcore/grid/distancemap.h:42-57, the GPU copy of
+ * cuda_addon/distancemap.cuh:6-116).  A map is a lattice of
+ * (cells[0]+1) x (cells[1]+1) x (cells[2]+1) vertices at vmin + i*cellSize
+ * holding a signed distance and the closest surface point; vertex (i,j,k)
+ * is entry k*(cx+1)*(cy+1) + j*(cx+1) + i. */
+typedef struct fcdemDistanceMap fcdemDistanceMap;
+
+/* Uploads a map given in the reference's host layout (distance[V],
+ * contactPoints[3V]); NULL arrays leave the vertices zero.  The device copy
+ * packs (distance, cp.x, cp.y, cp.z) per vertex, replacing
+ * DistanceMap<float,gpu>::transferData (distancemap.cuh:50-95). */
+fcdemDistanceMap *fcdemDistMapCreate(const float *distance, const float *contactPoints,
+                                     const float vmin[3], const float vmax[3],
+                                     float cellSize, const int cells[3]);
+/* A map of the torus around the z axis with major radius R and tube radius
+ * r, evaluated exactly at each vertex on the GPU: cellsPerAxis cubic cells
+ * across x and y over +-(R + r + margin), z rounded up to whole cells over
+ * +-(r + margin) (the cubic-cell rule of distancemap.cpp:180-229). */
+fcdemDistanceMap *fcdemDistMapTorus(float majorRadius, float tubeRadius, int cellsPerAxis,
+                                    float margin);
+void fcdemDistMapDestroy(fcdemDistanceMap *map);
+void fcdemDistMapGeometry(const fcdemDistanceMap *map, float vmin[3], float vmax[3],
+                          float *cellSize, int cells[3]);
+/* Copies the packed vertices (4 floats each) to host memory. */
+void fcdemDistMapVertices(const fcdemDistanceMap *map, float *vertices4);
+/* DistanceMap<float,gpu>::queryMap (distancemap.cuh:154-191) for n device
+ * points (4 floats each): trilinear distance (5.0 outside the box) and, if
+ * cp4 is not NULL, contact point.  A query on the upper face uses the last
+ * cell (the reference reads one vertex past the row there). */
+void fcdemDistMapQuery(const fcdemDistanceMap *map, const float *queries4, unsigned n,
+                       float *dist, float *cp4);
+
+/* particledem_um entry points (cuda_addon/particledem_um.cuh:11-27), with the
+ * work arrays as arguments instead of the file's global world and grid.
+ *
+ * particledem_um.cu:604-638 + boundaries.cuh:65-89: integrate, then the
+ * distance-map contact (map may be NULL: none), the r = 1 cylinder around z
+ * and the z planes -1 and 10; vel.w receives pos.w as in the reference. */
+void fcdemUM_integrateSystem(float *pos, float *vel, float deltaTime, uint numParticles,
+                             const fcdemDistanceMap *map);
+/* particledem_um.cu:457-602 (evalForces): collide without the collider
+ * sphere, newVel[index[i]] = (v + F, 0) and force[index[i]] = F (3 floats). */
+void fcdemUM_evalForces(float *newVel, float *force, float *sortedPos, float *sortedVel,
+                        uint *gridParticleIndex, uint *cellStart, uint *cellEnd,
+                        uint numParticles, uint numCells);
+/* particledem_um.cu:442-454: as reorderDataAndFindCellStart, with cellEnd
+ * reset to 0xffffffff first as well. */
+void fcdemUM_reorderDataAndFindCellStart(uint *cellStart, uint *cellEnd, float *sortedPos,
+                                         float *sortedVel, uint *gridParticleHash,
+                                         uint *gridParticleIndex, float *oldPos, float *oldVel,
+                                         uint numParticles, uint numCells);
+
+/* ---------------------------------------------------------------------- */
 /* Scene generators (host memory, 4 floats per particle).  Deterministic for
  * a given seed on every platform. */
 

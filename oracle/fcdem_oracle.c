@@ -419,18 +419,19 @@ void orc_distmap_query(const orc_distmap *m, const float q[3], float *dist,
   float xd = (q[0] - x0) / (x1 - x0);
   float yd = (q[1] - y0) / (y1 - y0);
   float zd = (q[2] - z0) / (z1 - z0);
-  /* trilinearInterpolateDistance, distancemap.cuh:227-252: the weights
-   * (1.0 - x_d) are double, so each level is evaluated in double and rounded
-   * to float on assignment. */
+  /* trilinearInterpolateDistance, distancemap.cuh:227-252.  In
+   * `d0 * (1.0 - x_d) + d1 * x_d` the first product is double (1.0 is a
+   * double literal), the second float * float; the sum is double and is
+   * rounded to float on assignment. */
   const float *D = m->distance;
   double wx = 1.0 - (double)xd, wy = 1.0 - (double)yd, wz = 1.0 - (double)zd;
-  float c00 = (float)((double)D[idx[0]] * wx + (double)D[idx[1]] * (double)xd);
-  float c10 = (float)((double)D[idx[3]] * wx + (double)D[idx[2]] * (double)xd);
-  float c01 = (float)((double)D[idx[4]] * wx + (double)D[idx[5]] * (double)xd);
-  float c11 = (float)((double)D[idx[7]] * wx + (double)D[idx[6]] * (double)xd);
-  float c0 = (float)((double)c00 * wy + (double)c10 * (double)yd);
-  float c1 = (float)((double)c01 * wy + (double)c11 * (double)yd);
-  *dist = (float)((double)c0 * wz + (double)c1 * (double)zd);
+  float c00 = (float)((double)D[idx[0]] * wx + (double)(D[idx[1]] * xd));
+  float c10 = (float)((double)D[idx[3]] * wx + (double)(D[idx[2]] * xd));
+  float c01 = (float)((double)D[idx[4]] * wx + (double)(D[idx[5]] * xd));
+  float c11 = (float)((double)D[idx[7]] * wx + (double)(D[idx[6]] * xd));
+  float c0 = (float)((double)c00 * wy + (double)(c10 * yd));
+  float c1 = (float)((double)c01 * wy + (double)(c11 * yd));
+  *dist = (float)((double)c0 * wz + (double)(c1 * zd));
   /* trilinearInterpolateCP, distancemap.cuh:254-279: Vector3<float> times a
    * float weight (the double weight converted to float). */
   const float *C = m->contactPoints;

@@ -164,6 +164,38 @@ def ref_gpu():
     return L
 
 
+def ref_distmap():
+    """The reference's own distance-map query and boundary response built as
+    host code (None if not built)."""
+    path = os.path.join(REF, "libfcref_distmap.so")
+    if not os.path.exists(path):
+        return None
+    L = _load("ref_distmap", path)
+    if not getattr(L, "_typed", False):
+        L.fcref_distmap_query.argtypes = [_f32p, _f32p, _f32p, _f32p, _f32p, C.c_float,
+                                          np.ctypeslib.ndpointer(dtype=np.int32,
+                                                                 flags="C_CONTIGUOUS"),
+                                          _f32p, C.c_int, _f32p, _f32p]
+        L.fcref_um_integrate.argtypes = [_f32p, _f32p, _f32p, _f32p, _f32p, _f32p, C.c_float,
+                                         np.ctypeslib.ndpointer(dtype=np.int32,
+                                                                flags="C_CONTIGUOUS"),
+                                         _f32p, _f32p, C.c_int, _f32p, C.c_float, C.c_float,
+                                         C.c_float, C.c_float]
+        L.fcref_distmap_query.restype = None
+        L.fcref_um_integrate.restype = None
+        L._typed = True
+    return L
+
+
+def lattice_coords(vmin, cell_size, cells):
+    """Vertex coordinates vmin + i*cellSize in float, vertex (i,j,k) at
+    k*(cx+1)*(cy+1) + j*(cx+1) + i (distancemap.cpp:214-226)."""
+    cs = np.float32(cell_size)
+    ax = [np.float32(vmin[k]) + np.arange(cells[k] + 1, dtype=np.float32) * cs for k in range(3)]
+    z, y, x = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+    return np.ascontiguousarray(np.stack([x, y, z], axis=-1).reshape(-1, 3).astype(np.float32))
+
+
 # ---------------------------------------------------------------------------
 # numpy-level helpers
 
