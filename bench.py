@@ -183,6 +183,24 @@ def dist_env():
     return world, rank, local
 
 
+def max_over_ranks(x: float, device="cpu") -> float:
+    """The largest of the ranks' values (the slowest replica's time); x itself
+    without a process group."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(n_per_rank: int, steps: int, seconds: float, world: int) -> float:
+    """Whole-job particle-steps/s of `world` replicas of n_per_rank particles
+    timed over `seconds` (the max over ranks)."""
+    return world * n_per_rank * steps / seconds
+
+
 def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
@@ -264,14 +282,9 @@ def run_ours(args):
     end.record()
     barrier()
     launches = int(lib.fcdemGetLaunchCount() - l0)
-    el_ms = start.elapsed_time(end)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([el_ms], device=f"cuda:{dev}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        el_ms = float(t.item())
+    el_ms = max_over_ranks(start.elapsed_time(end), f"cuda:{dev}")
     dem.check("timed updates")
-    value = world * n * args.steps / (el_ms / 1e3)
+    value = replica_throughput(n, args.steps, el_ms / 1e3, world)
 
     # --- stage attribution (same workload, events around each stage) -----
     lib.fcdemSetProfiling(1)
@@ -317,14 +330,9 @@ def run_ours(args):
         lib.copyArrayFromDevice(hpos.data_ptr(), ds.pos.data_ptr(), None, nbytes)
         lib.copyArrayFromDevice(hvel.data_ptr(), ds.vel.data_ptr(), None, nbytes)
     barrier()
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([e2e_s], device=f"cuda:{dev}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, f"cuda:{dev}")
     dem.check("e2e")
-    e2e = world * n * e2e_steps / e2e_s
+    e2e = replica_throughput(n, e2e_steps, e2e_s, world)
     clk = clocks.stop()
 
     cpu = None

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <vector>
 
@@ -147,6 +148,38 @@ extern "C" uint fcdemScenePack(float *pos4, float *vel4, uint n, const float box
     placed = i + 1;
   }
   return placed;
+}
+
+extern "C" int fcdemWriteVtkParticles(const char *path, const float *pos4, const float *vel4,
+                                      uint n, float radius, int radiusFromW) {
+  if (!path || (n && !pos4)) return FCDEM_ERR_INVALID_VALUE;
+  FILE *f = std::fopen(path, "w");
+  if (!f) return FCDEM_ERR_INVALID_VALUE;
+  std::fprintf(f, "# vtk DataFile Version 2.0\n");
+  std::fprintf(f, "Generated by fcdem-gb300\n");
+  std::fprintf(f, "ASCII\n");
+  std::fprintf(f, "DATASET UNSTRUCTURED_GRID\n");
+  std::fprintf(f, "POINTS %u double\n", n);
+  for (uint i = 0; i < n; ++i)
+    std::fprintf(f, "%f %f %f \n", pos4[4 * (size_t)i], pos4[4 * (size_t)i + 1],
+                 pos4[4 * (size_t)i + 2]);
+  std::fprintf(f, "POINT_DATA %u\n", n);
+  std::fprintf(f, "SCALARS radius double 1\n");
+  std::fprintf(f, "LOOKUP_TABLE default\n");
+  for (uint i = 0; i < n; ++i)
+    std::fprintf(f, "%f \n", radiusFromW ? pos4[4 * (size_t)i + 3] : radius);
+  std::fprintf(f, "SCALARS myid double 1\n");
+  std::fprintf(f, "LOOKUP_TABLE default\n");
+  for (uint i = 0; i < n; ++i) std::fprintf(f, "%f \n", (float)i);
+  if (vel4) {
+    std::fprintf(f, "VECTORS velocity double\n");
+    for (uint i = 0; i < n; ++i)
+      std::fprintf(f, "%f %f %f \n", vel4[4 * (size_t)i], vel4[4 * (size_t)i + 1],
+                   vel4[4 * (size_t)i + 2]);
+  }
+  int bad = std::ferror(f);
+  std::fclose(f);
+  return bad ? FCDEM_ERR_INVALID_VALUE : FCDEM_SUCCESS;
 }
 
 // ---------------------------------------------------------------------------

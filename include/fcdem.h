@@ -279,6 +279,16 @@ void fcdemUM_reorderDataAndFindCellStart(uint *cellStart, uint *cellEnd, float *
                                          uint *gridParticleIndex, float *oldPos, float *oldVel,
                                          uint numParticles, uint numCells);
 
+/* Particle output for ParaView, the format of CVtkWriter::WriteGPUParticleFile
+ * (inshape3dcore/postprocessing/vtkwriter.cpp:3399-3452): legacy ASCII
+ * UNSTRUCTURED_GRID with the positions of n particles (host array, 4 floats
+ * each), a "radius" scalar (pos.w when radiusFromW, else `radius`; the
+ * reference writes 1/64 for every particle) and a "myid" scalar.  When vel4 is
+ * not NULL a "velocity" vector is added.  Returns 0, or FCDEM_ERR_INVALID_VALUE
+ * when the file cannot be written. */
+int fcdemWriteVtkParticles(const char *path, const float *pos4, const float *vel4,
+                           uint n, float radius, int radiusFromW);
+
 /* ---------------------------------------------------------------------- */
 /* Scene generators (host memory, 4 floats per particle).  Deterministic for
  * a given seed on every platform. */

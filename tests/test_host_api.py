@@ -1,0 +1,83 @@
+"""Host-side pieces that need no GPU: the VTK particle writer, the C++
+particledem interface header (compiles and links against libfcdem.so), the
+scene generators."""
+import ctypes as C
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_vtk_writer_format(tmp_path):
+    from fullc0ntact_gb300 import _native
+    lib = _native.lib
+    lib.fcdemWriteVtkParticles.argtypes = [C.c_char_p, C.c_void_p, C.c_void_p, C.c_uint,
+                                           C.c_float, C.c_int]
+    lib.fcdemWriteVtkParticles.restype = C.c_int
+    pos = np.array([[0.5, -0.25, 1.0, 0.01], [0.0, 0.125, -0.5, 0.02]], np.float32)
+    vel = np.array([[1.0, 2.0, 3.0, 0.0], [4.0, 5.0, 6.0, 0.0]], np.float32)
+    path = str(tmp_path / "p.vtk")
+    assert lib.fcdemWriteVtkParticles(path.encode(), pos.ctypes.data, vel.ctypes.data, 2,
+                                      1.0 / 64.0, 1) == 0
+    lines = open(path).read().splitlines()
+    assert lines[:5] == ["# vtk DataFile Version 2.0", "Generated by fcdem-gb300", "ASCII",
+                         "DATASET UNSTRUCTURED_GRID", "POINTS 2 double"]
+    assert lines[5].split() == ["0.500000", "-0.250000", "1.000000"]
+    i = lines.index("SCALARS radius double 1")
+    assert [float(x) for x in lines[i + 2:i + 4]] == [0.01, 0.02]
+    i = lines.index("SCALARS myid double 1")
+    assert [float(x) for x in lines[i + 2:i + 4]] == [0.0, 1.0]
+    assert "VECTORS velocity double" in lines
+    assert lib.fcdemWriteVtkParticles(b"/nonexistent/dir/p.vtk", pos.ctypes.data, None, 2,
+                                      0.1, 0) != 0
+
+
+def test_particledem_header_compiles_and_links():
+    from fullc0ntact_gb300 import _native
+    src = r'''
+#include "fcdem_particledem.h"
+int main() {
+  fcdem::HashGrid hg; fcdem::ParticleWorld pw;
+  if (hg.size_ != 0 || pw.size_ != 0) return 1;
+  /* no GPU work: only check that every call resolves */
+  void (*a)(fcdem::HashGrid &, fcdem::ParticleWorld &) = fcdem::calcHash;
+  void (*b)(fcdem::HashGrid &) = fcdem::sortParticles;
+  void (*c)(fcdem::HashGrid &, fcdem::ParticleWorld &) = fcdem::reorderDataAndFindCellStart;
+  void (*d)(fcdem::HashGrid &, fcdem::ParticleWorld &) = fcdem::evalForces;
+  return (a && b && c && d) ? 0 : 2;
+}'''
+    with tempfile.TemporaryDirectory() as tmp:
+        cpp = os.path.join(tmp, "t.cpp")
+        open(cpp, "w").write(src)
+        exe = os.path.join(tmp, "t")
+        libdir = os.path.dirname(_native.LIB_PATH)
+        subprocess.run(["g++", "-std=c++17", "-I", os.path.join(ROOT, "include"), cpp, "-o", exe,
+                        "-L", libdir, "-lfcdem", f"-Wl,-rpath,{libdir}"], check=True)
+        assert subprocess.run([exe]).returncode == 0
+
+
+def test_packing_has_no_overlaps_and_reaches_density():
+    from fullc0ntact_gb300 import scenes
+    sc = scenes.config1(20000, grid=64)
+    p = sc["pos"].astype(np.float64)
+    r = p[:, 3]
+    assert r.max() <= 2.0 / 512.0 + 1e-9 and r.min() > 0
+    # brute force on a subset: no two spheres overlap
+    idx = np.random.default_rng(0).choice(len(p), 2000, replace=False)
+    d = np.linalg.norm(p[idx, None, :3] - p[None, :, :3], axis=2)
+    rr = r[idx, None] + r[None, :]
+    d[np.arange(2000), idx] = np.inf
+    assert np.all(d >= rr * (1 - 1e-6))
+    vf = (4.0 / 3.0 * np.pi * r ** 3).sum() / sc["box_side"] ** 3
+    assert 0.28 <= vf <= 0.31
+
+
+def test_scene_generators_are_deterministic():
+    from fullc0ntact_gb300 import scenes
+    a, b = scenes.config0(1000), scenes.config0(1000)
+    np.testing.assert_array_equal(a["pos"], b["pos"])
+    c, d = scenes.config1(3000, grid=32), scenes.config1(3000, grid=32)
+    np.testing.assert_array_equal(c["pos"], d["pos"])
