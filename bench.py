@@ -63,7 +63,7 @@ def load_scene(n: int) -> dict:
     """config1 scene, cached on local disk (packing 4M spheres takes ~15 s)."""
     from fullc0ntact_gb300 import scenes
     from fullc0ntact_gb300.params import SimParams
-    path = os.path.join(tempfile.gettempdir(), f"fcdem_scene_packed_{n}_v1.npz")
+    path = os.path.join(tempfile.gettempdir(), f"fcdem_scene_packed_{n}_v2.npz")
     if os.path.exists(path):
         try:
             with np.load(path) as z:

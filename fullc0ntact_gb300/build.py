@@ -22,6 +22,7 @@ SOURCES = [
     "fcdem_collide.cu",
     "fcdem_count.cu",
     "fcdem_distmap.cu",
+    "fcdem_batch.cu",
     "fcdem_host.cpp",
 ]
 

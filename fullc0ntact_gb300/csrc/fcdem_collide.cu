@@ -549,6 +549,67 @@ void launchT(bool tiled, bool cull, unsigned n, float4 *newVel, const float4 *sp
                                           ctx().dStatus);
 }
 
+// Batched collide (fcdem_batch.cu): slot i belongs to scene sceneOf[i]; its
+// parameters, box and cell offset come from scenes[].  Same arithmetic as
+// kCollideGlobal, the prefix table shifted by the scene's cellBase.
+template <int kMode, bool kRadiusFromW>
+__global__ void __launch_bounds__(128)
+kCollideBatch(const BatchScene *__restrict__ scenes, const unsigned *__restrict__ sceneOf,
+              float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
+              const float4 *__restrict__ sortedVel, const unsigned *__restrict__ index,
+              const unsigned *__restrict__ off, unsigned n, CollideOut out, unsigned *status) {
+  __shared__ unsigned qj[kQueueLen * kQueueStride];
+  __shared__ unsigned char qc[kQueueLen * kQueueStride];
+  unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const BatchScene &S = scenes[__ldg(sceneOf + i)];
+  const SimParams &P = S.p;
+  float4 p4 = ldg4(sortedPos + i);
+  float4 v4 = ldg4(sortedVel + i);
+  float3 pos = make_float3(p4.x, p4.y, p4.z), vel = make_float3(v4.x, v4.y, v4.z);
+  float ri = kRadiusFromW ? p4.w : P.particleRadius;
+  int3 g = gridPos(pos.x, pos.y, pos.z, P);
+  bool cull = S.cull != 0;
+  if (kRadiusFromW && !(ri <= P.particleRadius)) {
+    atomicOr(status, (unsigned)kStatusRadiusBound);
+    cull = false;
+  }
+  CellRanges cells;
+  cells.off = off + S.cellBase;
+  float3 force = neighbourForceGlobal<kRadiusFromW, true>(i, n, pos, vel, ri, g, cull,
+                                                          sortedPos, sortedVel, cells, P,
+                                                          qj + threadIdx.x, qc + threadIdx.x);
+  // collider sphere (particles_kernel.cu:288)
+  {
+    float3 rel = make_float3(P.colliderPos[0] - pos.x, P.colliderPos[1] - pos.y,
+                             P.colliderPos[2] - pos.z);
+    float dist = pairDist(rel);
+    float cd = ri + P.colliderRadius;
+    if (dist < cd) {
+      float3 f = contactTerm(rel, dist, cd, vel, make_float3(0.0f, 0.0f, 0.0f), 0.0f, P);
+      force.x = force.x + f.x;
+      force.y = force.y + f.y;
+      force.z = force.z + f.z;
+    }
+  }
+  float3 nv = make_float3(vel.x + force.x, vel.y + force.y, vel.z + force.z);
+  if (kMode == 2) {
+    integrateOneBox(pos, nv, out.dt, ri, P, S.lo, S.hi);
+    out.posOut[i] = make_float4(pos.x, pos.y, pos.z, p4.w);
+    newVel[i] = make_float4(nv.x, nv.y, nv.z, 0.0f);
+    int3 gn = gridPos(pos.x, pos.y, pos.z, P);
+    const unsigned h = S.cellBase + gridHash(gn.x, gn.y, gn.z, P);
+    out.hashOut[i] = h;
+    out.rankOut[i] = atomicAdd(out.cnt + h, 1u);
+    countTile(out.tileCnt, h >> 12);
+  } else {
+    unsigned o = __ldg(index + i);
+    if (o >= n) return;
+    newVel[o] = make_float4(nv.x, nv.y, nv.z, 0.0f);
+    out.posOut[o] = p4;
+  }
+}
+
 int g_collidePath = -1;  // -1 auto, 0 global, 1 tiled (fcdemSetCollidePath)
 bool g_cullCells = true;  // fcdemSetCellCulling
 
@@ -596,6 +657,28 @@ void launchCollide(int mode, bool collider, float4 *newVel, const float4 *sp,
   FCDEM_COLLIDE_CASE(3, true, true, false, true)
 #undef FCDEM_COLLIDE_CASE
   setError(FCDEM_ERR_INVALID_VALUE);
+}
+
+void launchCollideBatch(int mode, bool radiusFromW, const BatchScene *scenes,
+                        const unsigned *sceneOf, float4 *newVel, const float4 *sp,
+                        const float4 *sv, const unsigned *index, const unsigned *off,
+                        unsigned n, const CollideOut &out) {
+  if (n == 0) return;
+  const unsigned blocks = (n + 127) / 128;
+  unsigned *st = ctx().dStatus;
+  if (mode == 2 && !radiusFromW)
+    kCollideBatch<2, false><<<blocks, 128, 0, curStream()>>>(scenes, sceneOf, newVel, sp, sv,
+                                                             index, off, n, out, st);
+  else if (mode == 2)
+    kCollideBatch<2, true><<<blocks, 128, 0, curStream()>>>(scenes, sceneOf, newVel, sp, sv,
+                                                            index, off, n, out, st);
+  else if (!radiusFromW)
+    kCollideBatch<3, false><<<blocks, 128, 0, curStream()>>>(scenes, sceneOf, newVel, sp, sv,
+                                                             index, off, n, out, st);
+  else
+    kCollideBatch<3, true><<<blocks, 128, 0, curStream()>>>(scenes, sceneOf, newVel, sp, sv,
+                                                            index, off, n, out, st);
+  launchOk();
 }
 
 }  // namespace fcdem

@@ -300,33 +300,62 @@ kTileReduce(const unsigned *__restrict__ cnt, unsigned *__restrict__ tileCnt, un
 
 }  // namespace
 
+// First step of a batch: scene of particle i from sceneOf, integrate in the
+// scene's box, global cell id = the scene's cellBase + local hash.
+template <bool kRadiusFromW>
+__global__ void __launch_bounds__(256)
+kBatchIntegrateHashCount(const BatchScene *__restrict__ scenes,
+                         const unsigned *__restrict__ sceneOf, float4 *__restrict__ pos,
+                         float4 *__restrict__ vel, float dt, unsigned *__restrict__ hash,
+                         unsigned *__restrict__ rank, unsigned *__restrict__ cnt, unsigned n) {
+  unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const BatchScene &S = scenes[__ldg(sceneOf + i)];
+  const SimParams &P = S.p;
+  float4 p4 = pos[i], v4 = vel[i];
+  float3 p = make_float3(p4.x, p4.y, p4.z), v = make_float3(v4.x, v4.y, v4.z);
+  float r = kRadiusFromW ? p4.w : P.particleRadius;
+  integrateOneBox(p, v, dt, r, P, S.lo, S.hi);
+  pos[i] = make_float4(p.x, p.y, p.z, p4.w);
+  vel[i] = make_float4(v.x, v.y, v.z, v4.w);
+  int3 g = gridPos(p.x, p.y, p.z, P);
+  unsigned h = S.cellBase + gridHash(g.x, g.y, g.z, P);
+  hash[i] = h;
+  rank[i] = atomicAdd(cnt + h, 1u);
+}
+
 // Buffers of the pipeline, kept in the context between calls: cnt (all zero
 // between calls) and off over numCells + 1 cells, rank/slotKey/slotIdx over
 // the particles, and the scan's look-back words.
 static bool countBuffers(Context &c, unsigned n, unsigned numCells, CountBuffers &b) {
+  return countBuffersIn(c.countBuf, c.countBytes, c.countCells, n, numCells, b);
+}
+
+bool countBuffersIn(void *&buf, size_t &bytes, unsigned &cells, unsigned n, unsigned numCells,
+                    CountBuffers &b) {
   const size_t m = (size_t)numCells + 1;
   const unsigned tiles = (unsigned)((m + kScanTile - 1) / kScanTile);
   auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
   const size_t need = 2 * al(m * 4) + 4 * al((size_t)n * 4) + 2 * al((size_t)(tiles + 1) * 4);
-  if (c.countBuf == nullptr || c.countBytes < need || c.countCells != numCells) {
+  if (buf == nullptr || bytes < need || cells != numCells) {
     if (!cudaOk(cudaDeviceSynchronize())) return false;
-    if (c.countBuf) cudaFree(c.countBuf);
-    c.countBuf = nullptr;
-    c.countBytes = 0;
-    if (cudaMalloc(&c.countBuf, need) != cudaSuccess) {
+    if (buf) cudaFree(buf);
+    buf = nullptr;
+    bytes = 0;
+    if (cudaMalloc(&buf, need) != cudaSuccess) {
       cudaGetLastError();
-      c.countBuf = nullptr;
+      buf = nullptr;
       setError(FCDEM_ERR_ALLOC);
       return false;
     }
-    c.countBytes = need;
-    c.countCells = numCells;
-    if (!cudaOk(cudaMemset(c.countBuf, 0, need))) return false;  // cnt starts at zero
+    bytes = need;
+    cells = numCells;
+    if (!cudaOk(cudaMemset(buf, 0, need))) return false;  // cnt starts at zero
   }
   // The arrays that must stay zero between calls (cnt, tileCnt) sit first,
   // at offsets that depend on the cell count only, so that a call with
   // another particle count reuses them in place.
-  char *p = (char *)c.countBuf;
+  char *p = (char *)buf;
   b.cnt = (unsigned *)p;
   p += al(m * 4);
   b.tileCnt = (unsigned *)p;
@@ -351,6 +380,20 @@ bool countPipelineBegin(Context &c, float4 *pos, float4 *vel, float dt, unsigned
   if (!countBuffers(c, n, numCells, b)) return false;
   kIntegrateHashCount<<<(n + 255) / 256, 256, 0, curStream()>>>(pos, vel, dt, hash, b.rank,
                                                                 b.cnt, n, kp);
+  if (!launchOk()) return false;
+  kTileReduce<<<b.scanTiles, kScanThreads, 0, curStream()>>>(b.cnt, b.tileCnt, numCells + 1);
+  return launchOk();
+}
+
+bool countPipelineBeginBatch(const BatchScene *scenes, const unsigned *sceneOf, bool radiusFromW,
+                             float4 *pos, float4 *vel, float dt, unsigned *hash, unsigned n,
+                             unsigned numCells, const CountBuffers &b) {
+  if (radiusFromW)
+    kBatchIntegrateHashCount<true><<<(n + 255) / 256, 256, 0, curStream()>>>(
+        scenes, sceneOf, pos, vel, dt, hash, b.rank, b.cnt, n);
+  else
+    kBatchIntegrateHashCount<false><<<(n + 255) / 256, 256, 0, curStream()>>>(
+        scenes, sceneOf, pos, vel, dt, hash, b.rank, b.cnt, n);
   if (!launchOk()) return false;
   kTileReduce<<<b.scanTiles, kScanThreads, 0, curStream()>>>(b.cnt, b.tileCnt, numCells + 1);
   return launchOk();

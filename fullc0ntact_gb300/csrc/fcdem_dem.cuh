@@ -56,6 +56,29 @@ __device__ __forceinline__ void integrateOne(float3 &p, float3 &v, float dt,
   if (p.y < -1.0f + r) { p.y = -1.0f + r; v.y = v.y * bd; }
 }
 
+// integrateOne with the box [lo, hi] instead of the reference's [-1, 1]^3
+// (the batched scenes each have their own box); same faces in the same order.
+__device__ __forceinline__ void integrateOneBox(float3 &p, float3 &v, float dt, float r,
+                                                const SimParams &P, const float *lo,
+                                                const float *hi) {
+  v.x = v.x + P.gravity[0] * dt;
+  v.y = v.y + P.gravity[1] * dt;
+  v.z = v.z + P.gravity[2] * dt;
+  v.x = v.x * P.globalDamping;
+  v.y = v.y * P.globalDamping;
+  v.z = v.z * P.globalDamping;
+  p.x = p.x + v.x * dt;
+  p.y = p.y + v.y * dt;
+  p.z = p.z + v.z * dt;
+  const float bd = P.boundaryDamping;
+  if (p.x > hi[0] - r) { p.x = hi[0] - r; v.x = v.x * bd; }
+  if (p.x < lo[0] + r) { p.x = lo[0] + r; v.x = v.x * bd; }
+  if (p.y > hi[1] - r) { p.y = hi[1] - r; v.y = v.y * bd; }
+  if (p.z > hi[2] - r) { p.z = hi[2] - r; v.z = v.z * bd; }
+  if (p.z < lo[2] + r) { p.z = lo[2] + r; v.z = v.z * bd; }
+  if (p.y < lo[1] + r) { p.y = lo[1] + r; v.y = v.y * bd; }
+}
+
 // The force of particles_kernel.cu:185-218 (collideSpheres) once the
 // distance test has passed: rel = pB - pA, dist = |rel|, cd = rA + rB.
 __device__ __forceinline__ float3 contactTerm(float3 rel, float dist, float cd,

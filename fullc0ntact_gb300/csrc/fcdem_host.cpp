@@ -61,6 +61,23 @@ extern "C" uint fcdemScenePack(float *pos4, float *vel4, uint n, const float box
     double r = (double)rMedian * std::exp((double)sigma * z);
     radii[i] = (float)std::min(r, (double)rMax);
   }
+  return fcdemScenePackRadii(pos4, vel4, n, radii.data(), boxMin, boxMax, velRange, s,
+                             maxAttempts);
+}
+
+extern "C" uint fcdemScenePackRadii(float *pos4, float *vel4, uint n, const float *radiiIn,
+                                    const float boxMin[3], const float boxMax[3],
+                                    float velRange, unsigned long long seed,
+                                    uint maxAttempts) {
+  u64 s = seed;
+  std::vector<float> radii(radiiIn, radiiIn + n);
+  float rMax = 0.0f, rMedian = 0.0f;
+  for (uint i = 0; i < n; ++i) rMax = std::max(rMax, radii[i]);
+  if (n) {
+    std::vector<float> tmp(radii);
+    std::nth_element(tmp.begin(), tmp.begin() + n / 2, tmp.end());
+    rMedian = tmp[n / 2];
+  }
   // The box is filled slab by slab along z, each slab at least 8 rMax thick
   // and given a share of the spheres proportional to the height its centres
   // can use, largest first; a candidate is then tested only against spheres

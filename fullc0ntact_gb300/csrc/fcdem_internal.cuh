@@ -131,6 +131,24 @@ void launchCollide(int mode, bool collider, float4 *newVel, const float4 *sp,
                    const float4 *sv, const unsigned *index, const CellRanges &cells,
                    unsigned n, const KParams &kp, const CollideOut &out);
 
+// One scene of a batch (fcdem_batch.cu), on the device.
+struct BatchScene {
+  SimParams p;
+  float lo[3], hi[3];     // the scene's box (integrate clamps to it)
+  unsigned cellBase;      // global id of the scene's cell 0
+  unsigned particleBase;  // first particle of the scene
+  int cull;               // collide may cull cells (see launchCollide)
+  int pad;
+};
+
+// Batched collide: particles of many scenes in one launch; sceneOf[i] is
+// the scene of particle/slot i, cell ids are cellBase + local hash.  mode 2
+// (next integrate in the scene's box + hash + count at slot i) or 3 (last).
+void launchCollideBatch(int mode, bool radiusFromW, const BatchScene *scenes,
+                        const unsigned *sceneOf, float4 *newVel, const float4 *sp,
+                        const float4 *sv, const unsigned *index, const unsigned *off,
+                        unsigned n, const CollideOut &out);
+
 // The counting-sort pipeline of fcdemUpdate (fcdem_count.cu).
 struct CountBuffers {
   unsigned *cnt, *off, *rank, *slotKey, *slotIdx, *slotPrev;
@@ -139,6 +157,14 @@ struct CountBuffers {
 };
 bool countPipelineBegin(Context &c, float4 *pos, float4 *vel, float dt, unsigned *hash,
                         unsigned n, unsigned numCells, const KParams &kp, CountBuffers &b);
+// Buffers over explicit storage (a batch owns its own); cnt/tileCnt must be
+// zero on first use.
+bool countBuffersIn(void *&buf, size_t &bytes, unsigned &cells, unsigned n, unsigned numCells,
+                    CountBuffers &b);
+// First step of a batch: integrate in each scene's box + hash + count.
+bool countPipelineBeginBatch(const BatchScene *scenes, const unsigned *sceneOf, bool radiusFromW,
+                             float4 *pos, float4 *vel, float dt, unsigned *hash, unsigned n,
+                             unsigned numCells, const CountBuffers &b);
 bool countPipelineSort(Context &c, const CountBuffers &b, const unsigned *origOf,
                        const float4 *prevPos, const float4 *prevVel, unsigned *hash,
                        unsigned *index, float4 *sortedPos, float4 *sortedVel, unsigned n,

@@ -299,3 +299,69 @@ def um_reorder(cell_start, cell_end, sorted_pos, sorted_vel, hash_, index, old_p
     lib.fcdemUM_reorderDataAndFindCellStart(_p(cell_start), _p(cell_end), _p(sorted_pos),
                                             _p(sorted_vel), _p(hash_), _p(index), _p(old_pos),
                                             _p(old_vel), n, num_cells)
+
+
+# --- batches of scenes --------------------------------------------------------
+
+class _BatchScene(C.Structure):
+    _fields_ = [("params", SimParams), ("boxLo", C.c_float * 3), ("boxHi", C.c_float * 3),
+                ("numParticles", C.c_uint)]
+
+
+_B_SIGS = {
+    "fcdemBatchCreate": (C.c_void_p, [C.POINTER(_BatchScene), C.c_uint, C.c_int]),
+    "fcdemBatchDestroy": (None, [C.c_void_p]),
+    "fcdemBatchNumParticles": (C.c_uint, [C.c_void_p]),
+    "fcdemBatchNumCells": (C.c_uint, [C.c_void_p]),
+    "fcdemBatchUpdate": (None, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_uint,
+                                C.c_int]),
+}
+for _n, (_r, _a) in _B_SIGS.items():
+    getattr(lib, _n).restype = _r
+    getattr(lib, _n).argtypes = _a
+
+
+class Batch:
+    """Independent scenes stepped together (fcdemBatch*): scene dicts with
+    pos, vel, params, box_lo, box_hi; their particles concatenated on the
+    device in scene order."""
+
+    def __init__(self, scene_list: list, device: str | torch.device = "cuda"):
+        if not scene_list:
+            raise ValueError("empty batch")
+        w = {bool(s.get("radius_from_w", False)) for s in scene_list}
+        if len(w) != 1:
+            raise ValueError("all scenes of a batch share the radius mode")
+        self.radius_from_w = w.pop()
+        self.dt = float(scene_list[0].get("dt", 0.5))
+        arr = (_BatchScene * len(scene_list))()
+        for k, s in enumerate(scene_list):
+            arr[k].params = s["params"]
+            lo = s.get("box_lo", (-1.0, -1.0, -1.0))
+            hi = s.get("box_hi", (1.0, 1.0, 1.0))
+            arr[k].boxLo[:] = [float(x) for x in lo]
+            arr[k].boxHi[:] = [float(x) for x in hi]
+            arr[k].numParticles = int(s["pos"].shape[0])
+        self._h = lib.fcdemBatchCreate(arr, len(scene_list), int(self.radius_from_w))
+        check("fcdemBatchCreate")
+        if not self._h:
+            raise MemoryError("fcdemBatchCreate failed")
+        self.sizes = [int(s["pos"].shape[0]) for s in scene_list]
+        self.n = int(lib.fcdemBatchNumParticles(self._h))
+        self.num_cells = int(lib.fcdemBatchNumCells(self._h))
+        dev = torch.device(device)
+        self.pos = torch.from_numpy(np.concatenate([s["pos"] for s in scene_list])).to(dev)
+        self.vel = torch.from_numpy(np.concatenate([s["vel"] for s in scene_list])).to(dev)
+
+    def update(self, steps: int = 1, dt: float | None = None, graph: bool = True) -> None:
+        lib.fcdemBatchUpdate(self._h, _p(self.pos), _p(self.vel),
+                             self.dt if dt is None else dt, steps, int(graph))
+
+    def split(self, t: torch.Tensor) -> list:
+        return list(torch.split(t, self.sizes))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib.fcdemBatchDestroy(h)
+            self._h = None

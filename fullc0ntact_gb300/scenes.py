@@ -24,6 +24,9 @@ _lib.fcdemSceneLattice.restype = None
 _lib.fcdemScenePack.argtypes = [_f32p, _f32p, C.c_uint, _f32p, _f32p, C.c_float,
                                 C.c_float, C.c_float, C.c_float, C.c_ulonglong, C.c_uint]
 _lib.fcdemScenePack.restype = C.c_uint
+_lib.fcdemScenePackRadii.argtypes = [_f32p, _f32p, C.c_uint, _f32p, _f32p, _f32p, C.c_float,
+                                     C.c_ulonglong, C.c_uint]
+_lib.fcdemScenePackRadii.restype = C.c_uint
 
 
 def lattice(n: int, radius: float, jitter: float, vel_range: float, seed: int,
@@ -100,3 +103,54 @@ def random_box(n: int, grid=(16, 16, 16), radius: float = 1.0 / 16.0, seed: int 
     p = make_params(n, grid, radius, cell_size=cell, world_origin=origin)
     return dict(name=f"random-{n}", pos=pos, vel=vel, params=p, radius_from_w=poly,
                 dt=0.5)
+
+
+def pack_radii(radii: np.ndarray, box_min, box_max, vel_range: float, seed: int,
+               max_attempts: int = 20000):
+    n = radii.shape[0]
+    pos = np.zeros((n, 4), np.float32)
+    vel = np.zeros((n, 4), np.float32)
+    placed = _lib.fcdemScenePackRadii(pos, vel, n, np.ascontiguousarray(radii, np.float32),
+                                      np.asarray(box_min, np.float32),
+                                      np.asarray(box_max, np.float32), vel_range, seed,
+                                      max_attempts)
+    if placed != n:
+        raise RuntimeError(f"packing placed {placed} of {n} spheres")
+    return pos, vel
+
+
+def _pow2_at_least(x: int) -> int:
+    g = 1
+    while g < x:
+        g *= 2
+    return g
+
+
+def batch_scene(n: int, seed: int, volume_fraction: float = 0.25, r_min: float = 1.0 / 512.0,
+                r_max: float = 1.0 / 256.0) -> dict:
+    """One scene of the batched workload: n spheres with radii U[r_min, r_max]
+    packed at the volume fraction in a cube of side L centred at the origin,
+    which is also the scene's box; grid cells of 2 r_max, the grid the next
+    power of two of cells covering the box."""
+    rng = np.random.default_rng(seed)
+    radii = rng.uniform(r_min, r_max, n).astype(np.float32)
+    vol = float((4.0 / 3.0 * np.pi * radii.astype(np.float64) ** 3).sum())
+    side = (vol / volume_fraction) ** (1.0 / 3.0)
+    lo, hi = [-side / 2.0] * 3, [side / 2.0] * 3
+    pos, vel = pack_radii(radii, lo, hi, 0.01, seed + 1)
+    cell = 2.0 * r_max
+    g = max(4, _pow2_at_least(int(np.ceil(side / cell))))
+    p = make_params(n, (g, g, g), particle_radius=r_max, cell_size=cell,
+                    world_origin=(-side / 2.0,) * 3, collider_pos=(10.0, 10.0, 10.0),
+                    collider_radius=0.0)
+    return dict(name=f"batch-scene-{n}", pos=pos, vel=vel, params=p, radius_from_w=True,
+                dt=0.5, box_lo=np.array(lo, np.float32), box_hi=np.array(hi, np.float32))
+
+
+def batch_config3(num_scenes: int = 512, n_min: int = 1024, n_max: int = 65536,
+                  seed: int = 3) -> list:
+    """Batched plain DEM: scene sizes drawn log-uniform in [n_min, n_max]
+    (seeded), radii U[1/512, 1/256], 25% volume fraction per scene."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(n_min), np.log(n_max), num_scenes)).astype(np.int64)
+    return [batch_scene(int(n), seed * 100003 + k) for k, n in enumerate(sizes)]

@@ -279,6 +279,33 @@ void fcdemUM_reorderDataAndFindCellStart(uint *cellStart, uint *cellEnd, float *
                                          uint *gridParticleIndex, float *oldPos, float *oldVel,
                                          uint numParticles, uint numCells);
 
+/* ---------------------------------------------------------------------- */
+/* Batches: many independent scenes stepped together (no counterpart in the
+ * reference, which steps one ParticleSystem at a time).  Every scene has its
+ * own SimParams (grid, cell size, origin, contact parameters), its own box
+ * [boxLo, boxHi] that integrate clamps to (the reference's box is [-1,1]^3),
+ * and numParticles particles; the particle arrays of a batch are the scenes'
+ * arrays concatenated in scene order (4 floats per particle, device memory). */
+typedef struct fcdemBatchScene {
+  SimParams params;
+  float boxLo[3], boxHi[3];
+  uint numParticles;
+} fcdemBatchScene;
+typedef struct fcdemBatch fcdemBatch;
+
+/* radiusFromW applies to every scene (fcdemSetRadiusMode). */
+fcdemBatch *fcdemBatchCreate(const fcdemBatchScene *scenes, uint numScenes, int radiusFromW);
+void fcdemBatchDestroy(fcdemBatch *batch);
+uint fcdemBatchNumParticles(const fcdemBatch *batch);
+uint fcdemBatchNumCells(const fcdemBatch *batch);
+/* `steps` updates of every scene, each stage one launch over all particles.
+ * useGraph: the sequence is recorded as a CUDA graph on the first call (and
+ * again when pos, vel, deltaTime or steps change) and replayed.  The result
+ * equals `steps` ParticleSystem-style updates of each scene on its own (with
+ * the scene's box). */
+void fcdemBatchUpdate(fcdemBatch *batch, float *pos, float *vel, float deltaTime, uint steps,
+                      int useGraph);
+
 /* Particle output for ParaView, the format of CVtkWriter::WriteGPUParticleFile
  * (inshape3dcore/postprocessing/vtkwriter.cpp:3399-3452): legacy ASCII
  * UNSTRUCTURED_GRID with the positions of n particles (host array, 4 floats
@@ -299,6 +326,13 @@ int fcdemWriteVtkParticles(const char *path, const float *pos4, const float *vel
 void fcdemSceneLattice(float *pos4, float *vel4, uint n, float radius,
                        float spacing, float jitter, float velRange,
                        unsigned long long seed);
+
+/* Random sequential packing of n spheres with the given radii (host array)
+ * inside [boxMin, boxMax]; the radii are placed largest first within z slabs.
+ * pos.w = radius.  Returns the number placed. */
+uint fcdemScenePackRadii(float *pos4, float *vel4, uint n, const float *radii,
+                         const float boxMin[3], const float boxMax[3], float velRange,
+                         unsigned long long seed, uint maxAttempts);
 
 /* Random sequential packing of n spheres with lognormal radii (median rMedian,
  * log-sigma sigma, clipped to rMax) inside [boxMin, boxMax]; pos.w = radius.
