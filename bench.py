@@ -48,7 +48,10 @@ WORKLOAD = "plain DEM at scale: 4,194,304 lognormal spheres, 256^3 grid, 30% pac
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=500,
+                    help="steps of the job (the 4M-sphere scene is a 500-step job)")
+    ap.add_argument("--chunk", type=int, default=50,
+                    help="steps between the events that report step time along the job")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=4194304, help="particles (default: the full workload)")
@@ -56,6 +59,10 @@ def parse():
     ap.add_argument("--cpu-budget-s", type=float, default=150.0,
                     help="time cap of the reference arm's timed steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the batched-scenes measurement")
+    ap.add_argument("--batch-scenes", type=int, default=512)
+    ap.add_argument("--batch-steps", type=int, default=20)
     return ap.parse_args()
 
 
@@ -156,6 +163,82 @@ def profile_traffic(kernel: str, n: int):
         return float(d["dram_bytes_per_launch"]) * n / float(d["n"])
     except Exception:
         return None
+
+
+def load_batch(num_scenes: int) -> list:
+    """Batched workload (scene sizes log-uniform in [1024, 65536], radii
+    U[1/512, 1/256], 25% volume fraction per scene), cached on local disk."""
+    from fullc0ntact_gb300 import scenes
+    from fullc0ntact_gb300.params import SimParams
+    path = os.path.join(tempfile.gettempdir(), f"fcdem_batch_{num_scenes}_v1.npz")
+    if os.path.exists(path):
+        try:
+            with np.load(path) as z:
+                k = int(z["k"])
+                out = []
+                for i in range(k):
+                    out.append(dict(pos=z[f"pos{i}"], vel=z[f"vel{i}"],
+                                    params=SimParams.from_buffer_copy(z[f"par{i}"].tobytes()),
+                                    box_lo=z[f"lo{i}"], box_hi=z[f"hi{i}"],
+                                    radius_from_w=True, dt=0.5))
+                return out
+        except Exception:
+            pass
+    sl = scenes.batch_config3(num_scenes)
+    arrays = {"k": np.int64(len(sl))}
+    for i, sc in enumerate(sl):
+        arrays[f"pos{i}"] = sc["pos"]
+        arrays[f"vel{i}"] = sc["vel"]
+        arrays[f"par{i}"] = np.frombuffer(bytes(sc["params"]), np.uint8)
+        arrays[f"lo{i}"] = sc["box_lo"]
+        arrays[f"hi{i}"] = sc["box_hi"]
+    tmp = path + f".{os.getpid()}.tmp.npz"
+    np.savez(tmp, **arrays)
+    os.replace(tmp, path)
+    return sl
+
+
+def measure_batched(num_scenes: int, steps: int, dev: int) -> dict:
+    """The same scenes stepped (a) all together as one batch, replayed from a
+    CUDA graph, and (b) one scene after the other with its own launches (the
+    plain step): particle-steps/s of each, CUDA events on the stream."""
+    import torch
+    from fullc0ntact_gb300 import dem
+    sl = load_batch(num_scenes)
+    n_total = sum(s["pos"].shape[0] for s in sl)
+    batch = dem.Batch(sl, f"cuda:{dev}")
+    batch.update(2, graph=True)  # records the 2-step graph, warms up
+    batch.update(steps, graph=True)  # records the timed graph
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    batch.update(steps, graph=True)
+    e1.record()
+    torch.cuda.synchronize()
+    batched_ms = e0.elapsed_time(e1)
+    dem.check("batched")
+    singles = [dem.Batch([sc], f"cuda:{dev}") for sc in sl]
+    for b in singles:
+        b.update(1, graph=False)
+    torch.cuda.synchronize()
+    e0.record()
+    for b in singles:
+        b.update(steps, graph=False)
+    e1.record()
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1)
+    dem.check("plain per scene")
+    sizes = [s["pos"].shape[0] for s in sl]
+    bv = n_total * steps / (batched_ms / 1e3)
+    pv = n_total * steps / (plain_ms / 1e3)
+    return {"workload": f"{num_scenes} scenes, sizes log-uniform in [1024, 65536], radii "
+                        "U[1/512, 1/256], 25% volume fraction, own box and grid each",
+            "n_total": n_total, "scene_min": int(min(sizes)), "scene_max": int(max(sizes)),
+            "cells_total": batch.num_cells, "steps": steps,
+            "batched_graph": {"value": bv, "ms_per_step": batched_ms / steps},
+            "plain_per_scene": {"value": pv, "ms_per_step": plain_ms / steps},
+            "speedup": bv / pv, "unit": UNIT,
+            "equal_results": "bit-identical per scene (tests/test_gpu_batch.py)"}
 
 
 def cpu_baseline(sc: dict, steps: int) -> dict:
@@ -267,32 +350,58 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize()
 
+    # The job is K steps from the packed initial state; every measured phase
+    # (timed, stage attribution, end to end) starts from that state, so each
+    # covers the same steps.  Late in the job the pile, held up only by the
+    # soft contact springs (spring 0.5), collapses into a few very crowded
+    # cells whose collide cost grows with the square of their occupancy.
+    pos0, vel0 = ds.pos.clone(), ds.vel.clone()
+
+    def reset():
+        ds.pos.copy_(pos0)
+        ds.vel.copy_(vel0)
+
     clocks = ClockSampler(dev)
     clocks.start()
     for _ in range(max(args.warmup, 0)):
         ds.update(1)
     dem.check("warm-up")
+    reset()
 
     # --- device-resident timing: K fused updates -------------------------
-    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # events between chunks of the job give the step time along the job
+    chunk = max(1, min(args.chunk, args.steps))
+    bounds = list(range(0, args.steps, chunk)) + [args.steps]
+    evs = [torch.cuda.Event(enable_timing=True) for _ in bounds]
     barrier()
     l0 = lib.fcdemGetLaunchCount()
-    start.record()
-    ds.update(args.steps)
-    end.record()
+    evs[0].record()
+    for k in range(1, len(bounds)):
+        ds.update(bounds[k] - bounds[k - 1])
+        evs[k].record()
     barrier()
     launches = int(lib.fcdemGetLaunchCount() - l0)
-    el_ms = max_over_ranks(start.elapsed_time(end), f"cuda:{dev}")
+    el_ms = max_over_ranks(evs[0].elapsed_time(evs[-1]), f"cuda:{dev}")
     dem.check("timed updates")
     value = replica_throughput(n, args.steps, el_ms / 1e3, world)
+    phases = [{"steps": [bounds[k - 1], bounds[k]],
+               "ms_per_step": evs[k - 1].elapsed_time(evs[k]) / (bounds[k] - bounds[k - 1])}
+              for k in range(1, len(bounds))]
+    hcount = torch.bincount(ds.hash.long(), minlength=ds.num_cells)
+    final_cells = {"max_occupancy": int(hcount.max().item()),
+                   "cells_over_1024": int((hcount > 1024).sum().item()),
+                   "cells_over_64": int((hcount > 64).sum().item())}
+    del hcount
 
     # --- stage attribution (same workload, events around each stage) -----
+    reset()
     lib.fcdemSetProfiling(1)
     ds.update(args.steps)
     ms = (C.c_float * 5)()
     cnt = (C.c_uint * 5)()
     lib.fcdemGetStageTimes(ms, cnt, 5)
     lib.fcdemSetProfiling(0)
+    dem.check("stage attribution")
     stage_names = ["integrate_hash", "sort", "fill", "reorder", "collide"]
     stage_ms = {nm: (ms[k] / cnt[k] if cnt[k] else None) for k, nm in enumerate(stage_names)}
     occupied = int((ds.cell_start != -1).sum().item())
@@ -318,7 +427,7 @@ def run_ours(args):
     hpos.copy_(torch.from_numpy(sc["pos"]))
     hvel.copy_(torch.from_numpy(sc["vel"]))
     nbytes = n * 16
-    e2e_steps = max(1, min(args.steps, 50))
+    e2e_steps = args.steps
     ds.activate()
     barrier()
     t0 = time.perf_counter()
@@ -335,6 +444,12 @@ def run_ours(args):
     e2e = replica_throughput(n, e2e_steps, e2e_s, world)
     clk = clocks.stop()
 
+    batched = None
+    if not args.no_batched:
+        del ds  # free the large scene's arrays first
+        torch.cuda.empty_cache()
+        batched = measure_batched(args.batch_scenes, args.batch_steps, dev)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline and world == 1:
         cpu = cpu_baseline(sc, args.cpu_steps)
@@ -345,7 +460,8 @@ def run_ours(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": el_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded packing)",
-            "config": {"workload": WORKLOAD, "n": n, "grid": 256, "cells": ncell,
+            "config": {"workload": f"{WORKLOAD}, {args.steps}-step job from the packed state",
+                       "n": n, "grid": 256, "cells": ncell,
                        "occupied_cells": occupied, "step": "fcdemUpdate (fused update)",
                        "sort_config": sort_cfg,
                        "l2": "inputs larger than L2 (no flush)",
@@ -360,6 +476,9 @@ def run_ours(args):
                          "traffic": traffic, "algorithmic_bytes": algo[dominant],
                          "avg_launch_ms": stage_ms[dominant]},
             "stage_ms": stage_ms,
+            "phases": phases,
+            "final_cells": final_cells,
+            "batched": batched,
             "clocks": clk,
             "cpu_baseline": cpu,
         }

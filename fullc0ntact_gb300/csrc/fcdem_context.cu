@@ -248,7 +248,7 @@ const char *fcdemGetErrorString(int code) {
     case FCDEM_ERR_KEY_RANGE: return "sort key above the grid's key width";
     case FCDEM_ERR_ALLOC: return "device allocation failed";
     case FCDEM_ERR_CELL_OVERFLOW:
-      return "fcdemUpdate: a cell holds more than 4096 particles (order inside it not stable)";
+      return "fcdemUpdate: the list of crowded cells overflowed (order inside a cell not stable)";
     case FCDEM_ERR_RADIUS_BOUND:
       return "radius-from-w mode: a particle radius exceeds SimParams.particleRadius";
     default: return "unknown error";

@@ -24,9 +24,11 @@
 //
 // The collide kernel reads `off` instead of cellStart/cellEnd.  At the end of
 // fcdemUpdate kCellTables writes cellStart/cellEnd from `off`, so every array
-// holds what the reference's stages leave.  Cells with more than
-// kFixupMaxCell members keep the atomic order and raise kStatusCellOverflow
-// (such a cell makes the reference's collide quadratic in it as well).
+// holds what the reference's stages leave.  A cell with more than
+// kFixupMaxCell members is left out of the per-slot re-rank (its cost grows
+// with the square of the cell) and listed instead; kFixupLarge then gives each
+// listed cell one CTA that sorts its members by particle index with a stable
+// block radix sort, whatever the cell's size.
 #include "fcdem_dem.cuh"
 
 namespace fcdem {
@@ -43,11 +45,15 @@ static_assert((1 << kTileShift) == kScanTile, "tile shift");
 // tileOff[t] = sum of tileCnt[0..t), tileOff[tiles] = the total; tileCnt is
 // cleared for the next step.  One CTA of 1024 threads, tiles in chunks.
 __global__ void __launch_bounds__(1024)
-kScanTiles(unsigned *__restrict__ tileCnt, unsigned *__restrict__ tileOff, unsigned tiles) {
+kScanTiles(unsigned *__restrict__ tileCnt, unsigned *__restrict__ tileOff, unsigned tiles,
+           unsigned *__restrict__ largeCount) {
   __shared__ unsigned sWarp[32];
   __shared__ unsigned sCarry;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) sCarry = 0;
+  if (tid == 0) {
+    sCarry = 0;
+    *largeCount = 0u;  // the fix-up lists this step's large cells afresh
+  }
   __syncthreads();
   for (unsigned base = 0; base < tiles; base += 1024) {
     const unsigned t = base + tid;
@@ -196,18 +202,27 @@ kScatterCells(const unsigned *__restrict__ hashN, const unsigned *__restrict__ r
   slotPrev[s] = i;
 }
 
-constexpr unsigned kFixupMaxCell = 4096;
+// Largest cell that the per-slot re-rank handles (each slot reads every
+// member of its cell).
+constexpr unsigned kFixupMaxCell = 1024;
+
+// Capacity of the large-cell list: a listed cell has more than kFixupMaxCell
+// of the n particles, so at most n / (kFixupMaxCell + 1) cells are listed.
+inline unsigned largeCapacity(unsigned n) { return n / (kFixupMaxCell + 1) + 1; }
 
 // Stable order inside each cell + the reorder gather.  The particle of slot
 // s is re-ranked among its cell's members by particle index; its position and
-// velocity are gathered from entry slotPrev[s] of the previous order.
+// velocity are gathered from entry slotPrev[s] of the previous order.  A cell
+// above kFixupMaxCell members is appended to large[1..] (large[0] counts) by
+// its first slot and left to kFixupLarge.
 __global__ void __launch_bounds__(256)
 kFixupGather(const unsigned *__restrict__ slotKey, const unsigned *__restrict__ slotOrig,
              const unsigned *__restrict__ slotPrev, const unsigned *__restrict__ off,
              unsigned *__restrict__ hashOut, unsigned *__restrict__ indexOut,
              float4 *__restrict__ sortedPos, float4 *__restrict__ sortedVel,
              const float4 *__restrict__ prevPos, const float4 *__restrict__ prevVel,
-             unsigned n, unsigned numCells, unsigned *status) {
+             unsigned n, unsigned numCells, unsigned *__restrict__ large, unsigned largeCap,
+             unsigned *status) {
   unsigned s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   const unsigned h = __ldg(slotKey + s);
@@ -215,19 +230,143 @@ kFixupGather(const unsigned *__restrict__ slotKey, const unsigned *__restrict__ 
   const unsigned prev = __ldg(slotPrev + s);
   if (h >= numCells || me >= n || prev >= n) return;  // unfilled slot (reported)
   const unsigned a = __ldg(off + h), b = __ldg(off + h + 1);
-  unsigned dst = s;
-  if (b - a <= kFixupMaxCell) {
-    unsigned r = 0;
-    for (unsigned t = a; t < b; ++t) r += __ldg(slotOrig + t) < me ? 1u : 0u;
-    dst = a + r;
-  } else if (s == a) {
-    atomicOr(status, (unsigned)kStatusCellOverflow);
+  if (b - a > kFixupMaxCell) {
+    if (s == a) {
+      const unsigned k = atomicAdd(large, 1u);
+      if (k < largeCap)
+        large[1 + k] = h;
+      else
+        atomicOr(status, (unsigned)kStatusCellOverflow);
+    }
+    return;
   }
+  unsigned r = 0;
+  for (unsigned t = a; t < b; ++t) r += __ldg(slotOrig + t) < me ? 1u : 0u;
+  const unsigned dst = a + r;
   if (dst >= n) return;
   hashOut[dst] = h;
   indexOut[dst] = me;
   sortedPos[dst] = ldg4(prevPos + prev);
   sortedVel[dst] = ldg4(prevVel + prev);
+}
+
+constexpr int kLargeThreads = 1024;
+constexpr int kLargeWarps = kLargeThreads / 32;
+constexpr int kLargeCtas = 152;
+
+struct LargeSmem {
+  unsigned bin[256];                  // running base of each digit
+  unsigned total[256];                // a chunk's count of each digit
+  unsigned part[8];                   // warp totals of the digit scan
+  unsigned warpCnt[kLargeWarps][256]; // per-warp digit counts of a chunk
+};
+
+// One stable pass of a block-wide LSD radix sort: src[0..c) -> dst[0..c)
+// by the 8-bit digit at bit `shift`.  Chunks of kLargeThreads entries go in
+// order; inside a chunk an entry's place is its digit's running base + the
+// count of that digit in earlier warps + its rank among its warp's peers.
+__device__ void largeRadixPass(const unsigned long long *src, unsigned long long *dst,
+                               unsigned c, int shift, LargeSmem &sm) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid < 256) sm.bin[tid] = 0u;
+  __syncthreads();
+  for (unsigned t = tid; t < c; t += kLargeThreads)
+    atomicAdd(&sm.bin[(unsigned)(src[t] >> shift) & 255u], 1u);
+  __syncthreads();
+  unsigned v = 0, x = 0;
+  if (tid < 256) {  // exclusive scan of the 256 digit counts, warps 0..7
+    v = sm.bin[tid];
+    x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) sm.part[warp] = x;
+  }
+  __syncthreads();
+  if (tid < 256) {
+    unsigned before = 0;
+    for (int w = 0; w < warp; ++w) before += sm.part[w];
+    sm.bin[tid] = before + x - v;
+  }
+  __syncthreads();
+  const unsigned lt = (1u << lane) - 1u;
+  for (unsigned base = 0; base < c; base += kLargeThreads) {
+    for (int q = tid; q < kLargeWarps * 256; q += kLargeThreads) (&sm.warpCnt[0][0])[q] = 0u;
+    __syncthreads();
+    const unsigned t = base + tid;
+    const bool valid = t < c;
+    const unsigned long long e = valid ? src[t] : 0ull;
+    const unsigned d = valid ? ((unsigned)(e >> shift) & 255u) : 256u;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const unsigned rank = __popc(peers & lt);
+    if (valid && rank == 0) sm.warpCnt[warp][d] = __popc(peers);
+    __syncthreads();
+    if (tid < 256) {  // per digit: exclusive prefix over the warps
+      unsigned run = 0;
+      for (int w = 0; w < kLargeWarps; ++w) {
+        const unsigned k = sm.warpCnt[w][tid];
+        sm.warpCnt[w][tid] = run;
+        run += k;
+      }
+      sm.total[tid] = run;
+    }
+    __syncthreads();
+    if (valid) dst[sm.bin[d] + sm.warpCnt[warp][d] + rank] = e;
+    __syncthreads();
+    if (tid < 256) sm.bin[tid] += sm.total[tid];
+    __syncthreads();
+  }
+}
+
+// The large cells listed by kFixupGather, one CTA per cell at a time.  The
+// members (particle index, previous entry) are sorted by particle index in
+// the cell's own range of sortedPos (16 bytes per member: two 8-byte arrays
+// of the cell's size), written back to slotOrig/slotPrev, then gathered as
+// in kFixupGather.  idBits = bits of the largest particle index.
+__global__ void __launch_bounds__(kLargeThreads)
+kFixupLarge(unsigned *__restrict__ slotOrig, unsigned *__restrict__ slotPrev,
+            const unsigned *__restrict__ off, const unsigned *__restrict__ large,
+            unsigned largeCap, unsigned *__restrict__ hashOut, unsigned *__restrict__ indexOut,
+            float4 *__restrict__ sortedPos, float4 *__restrict__ sortedVel,
+            const float4 *__restrict__ prevPos, const float4 *__restrict__ prevVel, unsigned n,
+            int idBits) {
+  __shared__ LargeSmem sm;
+  const unsigned count = min(large[0], largeCap);
+  const int tid = threadIdx.x;
+  for (unsigned k = blockIdx.x; k < count; k += gridDim.x) {
+    const unsigned h = large[1 + k];
+    const unsigned a = off[h], b = off[h + 1];
+    if (b > n || a >= b) continue;  // cannot happen for a listed cell
+    const unsigned c = b - a;
+    unsigned long long *A = reinterpret_cast<unsigned long long *>(sortedPos + a);
+    unsigned long long *B = A + c;
+    for (unsigned t = tid; t < c; t += kLargeThreads)
+      A[t] = ((unsigned long long)slotOrig[a + t] << 32) | slotPrev[a + t];
+    __syncthreads();
+    for (int shift = 0; shift < idBits; shift += 8) {
+      largeRadixPass(A, B, c, 32 + shift, sm);
+      unsigned long long *tmp = A;
+      A = B;
+      B = tmp;
+    }
+    for (unsigned t = tid; t < c; t += kLargeThreads) {
+      const unsigned long long e = A[t];
+      slotOrig[a + t] = (unsigned)(e >> 32);
+      slotPrev[a + t] = (unsigned)e;
+    }
+    __syncthreads();
+    for (unsigned t = tid; t < c; t += kLargeThreads) {
+      const unsigned me = slotOrig[a + t], prev = slotPrev[a + t];
+      if (me >= n || prev >= n) continue;  // unfilled slot (reported by the scatter)
+      hashOut[a + t] = h;
+      indexOut[a + t] = me;
+      sortedPos[a + t] = ldg4(prevPos + prev);
+      sortedVel[a + t] = ldg4(prevVel + prev);
+    }
+    __syncthreads();
+  }
 }
 
 // cellStart/cellEnd from the prefix table (cellEnd of empty cells untouched,
@@ -336,7 +475,9 @@ bool countBuffersIn(void *&buf, size_t &bytes, unsigned &cells, unsigned n, unsi
   const size_t m = (size_t)numCells + 1;
   const unsigned tiles = (unsigned)((m + kScanTile - 1) / kScanTile);
   auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
-  const size_t need = 2 * al(m * 4) + 4 * al((size_t)n * 4) + 2 * al((size_t)(tiles + 1) * 4);
+  const unsigned largeCap = largeCapacity(n);
+  const size_t need = 2 * al(m * 4) + 4 * al((size_t)n * 4) + 2 * al((size_t)(tiles + 1) * 4) +
+                      al(((size_t)largeCap + 1) * 4);
   if (buf == nullptr || bytes < need || cells != numCells) {
     if (!cudaOk(cudaDeviceSynchronize())) return false;
     if (buf) cudaFree(buf);
@@ -371,6 +512,9 @@ bool countBuffersIn(void *&buf, size_t &bytes, unsigned &cells, unsigned n, unsi
   b.slotIdx = (unsigned *)p;
   p += al((size_t)n * 4);
   b.slotPrev = (unsigned *)p;
+  p += al((size_t)n * 4);
+  b.large = (unsigned *)p;
+  b.largeCap = largeCap;
   b.scanTiles = tiles;
   return true;
 }
@@ -408,7 +552,7 @@ bool countPipelineSort(Context &c, const CountBuffers &b, const unsigned *origOf
                        unsigned numCells) {
   cudaStream_t st = curStream();
   const unsigned m = numCells + 1;
-  kScanTiles<<<1, 1024, 0, st>>>(b.tileCnt, b.tileOff, b.scanTiles);
+  kScanTiles<<<1, 1024, 0, st>>>(b.tileCnt, b.tileOff, b.scanTiles, b.large);
   if (!launchOk()) return false;
   kScanCells<<<b.scanTiles, kScanThreads, 0, st>>>(b.cnt, b.off, m, b.tileOff);
   if (!launchOk()) return false;
@@ -419,7 +563,13 @@ bool countPipelineSort(Context &c, const CountBuffers &b, const unsigned *origOf
   if (!launchOk()) return false;
   kFixupGather<<<(n + 255) / 256, 256, 0, st>>>(b.slotKey, b.slotIdx, b.slotPrev, b.off, hash,
                                                  index, sortedPos, sortedVel, prevPos, prevVel,
-                                                 n, numCells, c.dStatus);
+                                                 n, numCells, b.large, b.largeCap, c.dStatus);
+  if (!launchOk()) return false;
+  // Returns at once when the fix-up listed no cell (the common case).
+  const unsigned largeCtas = b.largeCap < (unsigned)kLargeCtas ? b.largeCap : kLargeCtas;
+  kFixupLarge<<<largeCtas, kLargeThreads, 0, st>>>(b.slotIdx, b.slotPrev, b.off, b.large,
+                                                   b.largeCap, hash, index, sortedPos,
+                                                   sortedVel, prevPos, prevVel, n, keyBits(n));
   return launchOk();
 }
 

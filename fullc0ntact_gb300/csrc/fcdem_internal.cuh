@@ -31,7 +31,7 @@ enum : unsigned {
   kStatusTimeout = 1u,   // a bounded spin-wait gave up
   kStatusKeyRange = 2u,  // a sort key had bits above the sorted width
   kStatusRadiusBound = 4u,  // radius-from-w mode: a radius above particleRadius
-  kStatusCellOverflow = 8u,  // counting sort: a cell too full for the stable fix-up
+  kStatusCellOverflow = 8u,  // counting sort: the list of crowded cells overflowed
 };
 
 // Everything a kernel needs from the parameter block, passed by value so
@@ -153,7 +153,8 @@ void launchCollideBatch(int mode, bool radiusFromW, const BatchScene *scenes,
 struct CountBuffers {
   unsigned *cnt, *off, *rank, *slotKey, *slotIdx, *slotPrev;
   unsigned *tileCnt, *tileOff;  // per 4096-cell tile: counts and their prefix
-  unsigned scanTiles;
+  unsigned *large;              // [0] = count, [1..largeCap] = cells too full for the re-rank
+  unsigned scanTiles, largeCap;
 };
 bool countPipelineBegin(Context &c, float4 *pos, float4 *vel, float dt, unsigned *hash,
                         unsigned n, unsigned numCells, const KParams &kp, CountBuffers &b);

@@ -153,7 +153,7 @@ void collide(float *newVel, float *sortedPos, float *sortedVel,
 #define FCDEM_ERR_KEY_RANGE         6  /* sort key above the grid's key width */
 #define FCDEM_ERR_ALLOC             7  /* device scratch allocation failed    */
 #define FCDEM_ERR_RADIUS_BOUND      8  /* a radius above particleRadius (w mode) */
-#define FCDEM_ERR_CELL_OVERFLOW     9  /* fcdemUpdate: > 4096 particles in a cell */
+#define FCDEM_ERR_CELL_OVERFLOW     9  /* fcdemUpdate: large-cell list overflowed (internal) */
 
 /* Returns and clears the first error recorded since the last call.  It
  * synchronises the library stream so that device-side status words (bounded

@@ -135,3 +135,35 @@ def test_counting_pipeline_on_packed_scene_and_crowded_cells():
         dem.check("update")
         for x, y in zip(_state(a), _state(b)):
             np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
+
+
+@pytest.mark.parametrize("n,grid", [(6000, 8), (100_000, 128)])
+def test_counting_pipeline_cells_above_rerank_limit(n, grid):
+    """Cells holding more than the per-slot re-rank handles (1,024) go to the
+    block radix sort of their members; the result stays identical to the
+    staged radix-sort path.  n = 100,000 needs three 8-bit passes over the
+    particle index, n = 6,000 two."""
+    from fullc0ntact_gb300 import dem, scenes
+    if grid == 8:
+        sc = scenes.random_box(n, grid=(8, 8, 8), radius=0.02, cell=0.25, seed=11)
+    else:
+        sc = scenes.config1(n, grid=grid)
+    rng = np.random.default_rng(5)
+    cell = float(sc["params"].cellSize[0])
+    origin = np.array([sc["params"].worldOrigin[k] for k in range(3)], np.float32)
+    # three crowded cells: 3,000 / 1,500 / 1,025 members (two of them in the
+    # same neighbourhood), drawn from scattered particle indices
+    picks = rng.permutation(n)
+    start = 0
+    for count, c in ((3000, (3, 3, 3)), (1500, (4, 3, 3)), (1025, (6, 6, 6))):
+        idx = picks[start:start + count]
+        start += count
+        lo = origin + np.array(c, np.float32) * cell
+        sc["pos"][idx, :3] = lo + rng.uniform(0.2, 0.8, (count, 3)).astype(np.float32) * cell
+    a, b = dem.DeviceScene(sc), dem.DeviceScene(sc)
+    for _ in range(2):
+        a.stages()
+    b.update(2)
+    dem.check("update")
+    for x, y in zip(_state(a), _state(b)):
+        np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
