@@ -52,6 +52,8 @@ _SIGS = {
     "fcdemVersion": (C.c_char_p, []),
     "fcdemSetCollidePath": (None, [C.c_int]),
     "fcdemSetCellCulling": (None, [C.c_int]),
+    "fcdemSetCrowdPath": (None, [C.c_int]),
+    "fcdemSetCrowdLimit": (None, [C.c_uint]),
     "fcdemSetUpdatePipeline": (None, [C.c_int]),
     "fcdemAutotuneSort": (C.c_int, [C.c_uint, C.c_uint, C.POINTER(C.c_float)]),
     "fcdemSetSortConfig": (C.c_int, [C.c_uint, C.c_int]),

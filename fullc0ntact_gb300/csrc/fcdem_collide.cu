@@ -292,12 +292,85 @@ __device__ __forceinline__ float3 neighbourForceGlobal(
   return force;
 }
 
+// ---------------------------------------------------------------------------
+// Crowded neighbourhoods.  When a particle's 27 neighbour cells hold more
+// than kCrowdLimit particles (a collapsed pile), one thread walking them all
+// is a long serial loop and the few warps that hold such particles leave the
+// SMs idle.  kCollideGlobal then defers the particle: the members of its
+// cell are listed in groups of up to 32 consecutive sorted particles (the
+// member at offset 0, 32, 64 ... of the cell appends its group), and
+// kCollideCrowd gives each group one warp, groups handed out dynamically.
+// The lanes of a group share their 27 neighbour cells, so they walk the same
+// partner sequence: every partner load is one broadcast, no lane diverges
+// in its loop bounds, and each lane still sums its own terms cell by cell in
+// ascending partner order -- the reference's arithmetic.
+constexpr unsigned kCrowdLimit = 1024;
+constexpr int kCrowdWarps = 8;
+
+struct CrowdList {
+  unsigned *count;  // [0] groups listed, [1] groups handed out past the first round
+  uint2 *groups;    // (first sorted particle, members); nullptr: path off
+  unsigned cap;
+  unsigned limit;   // neighbourhood size above which a particle is deferred
+};
+
+// Range [a, b) of cell h (empty: a == b).
+template <bool kPrefix>
+__device__ __forceinline__ void cellRange(unsigned h, const CellRanges &cells, unsigned n,
+                                          unsigned &a, unsigned &b) {
+  if (kPrefix) {
+    a = __ldg(cells.off + h);
+    b = min(__ldg(cells.off + h + 1), n);
+  } else {
+    a = __ldg(cells.start + h);
+    if (a == kEmpty) {
+      a = 0u;
+      b = 0u;
+    } else {
+      b = min(__ldg(cells.end + h), n);
+    }
+  }
+  if (b < a) b = a;
+}
+
+// Particles in the 27 neighbour cells of grid position g.  The nine rows
+// are independent (no early exit), so their table loads overlap.
+template <bool kPrefix>
+__device__ __forceinline__ unsigned neighbourhoodCount(int3 g, const CellRanges &cells,
+                                                       unsigned n, const SimParams &P) {
+  unsigned total = 0;
+  const unsigned gxm = P.gridSize[0] - 1u;
+  const unsigned xm = (unsigned)(g.x) & gxm;
+  if (kPrefix && xm >= 1u && xm < gxm) {
+    // no x wrap: each row's three cells are consecutive hashes
+#pragma unroll
+    for (int row = 0; row < 9; row++) {
+      const int z = row / 3 - 1, y = row % 3 - 1;
+      const unsigned h0 = gridHash(g.x - 1, g.y + y, g.z + z, P);
+      const unsigned o0 = __ldg(cells.off + h0), o3 = __ldg(cells.off + h0 + 3);
+      total += o3 > o0 ? o3 - o0 : 0u;
+    }
+    return total;
+  }
+#pragma unroll 1
+  for (int row = 0; row < 9; row++) {
+    const int z = row / 3 - 1, y = row % 3 - 1;
+#pragma unroll
+    for (int x = 0; x < 3; x++) {
+      unsigned a, b;
+      cellRange<kPrefix>(gridHash(g.x + x - 1, g.y + y, g.z + z, P), cells, n, a, b);
+      total += b - a;
+    }
+  }
+  return total;
+}
+
 template <int kMode, bool kRadiusFromW, bool kCollider, bool kForceOut, bool kPrefix>
 __global__ void __launch_bounds__(128)
 kCollideGlobal(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
                const float4 *__restrict__ sortedVel, const unsigned *__restrict__ index,
                CellRanges cells, unsigned n, KParams kp, CollideOut out, bool cull,
-               unsigned *status) {
+               CrowdList crowd, unsigned *status) {
   __shared__ unsigned qj[kQueueLen * kQueueStride];
   __shared__ unsigned char qc[kQueueLen * kQueueStride];
   const SimParams &P = kp.p;
@@ -308,6 +381,18 @@ kCollideGlobal(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos
   float3 pos = make_float3(p4.x, p4.y, p4.z), vel = make_float3(v4.x, v4.y, v4.z);
   float ri = kRadiusFromW ? p4.w : P.particleRadius;
   int3 g = gridPos(pos.x, pos.y, pos.z, P);
+  if (crowd.groups &&
+      neighbourhoodCount<kPrefix>(g, cells, n, P) > crowd.limit) {
+    unsigned a, b;
+    cellRange<kPrefix>(gridHash(g.x, g.y, g.z, P), cells, n, a, b);
+    if (i >= a && i < b) {  // deferred to kCollideCrowd
+      if (((i - a) & 31u) == 0u) {
+        const unsigned k = atomicAdd(crowd.count, 1u);
+        if (k < crowd.cap) crowd.groups[k] = make_uint2(i, min(32u, b - i));
+      }
+      return;
+    }
+  }
   if (kRadiusFromW && !(ri <= P.particleRadius)) {  // the culling bound is broken
     atomicOr(status, (unsigned)kStatusRadiusBound);
     cull = false;
@@ -317,6 +402,129 @@ kCollideGlobal(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos
       qc + threadIdx.x);
   finishParticle<kMode, kCollider, kForceOut>(i, n, pos, vel, p4, ri, force, index, newVel,
                                               out, P);
+}
+
+// One warp per listed group (see CrowdList).  Warp w first takes group w,
+// then further groups from a shared counter.  A neighbour cell is walked in
+// chunks of 32 partners: each lane loads one partner's position and velocity
+// (one coalesced load per chunk, the next chunk's issued before the current
+// one is used) into the warp's shared-memory chunk; the scan reads the chunk
+// with broadcast loads, tests the squared distance and queues each lane's
+// near partners in order; the drain then runs the exact test and the contact
+// terms with the lanes that have queued partners, all from shared memory.
+template <int kMode, bool kRadiusFromW, bool kCollider, bool kForceOut, bool kPrefix>
+__global__ void __launch_bounds__(kCrowdWarps * 32)
+kCollideCrowd(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
+              const float4 *__restrict__ sortedVel, const unsigned *__restrict__ index,
+              CellRanges cells, unsigned n, KParams kp, CollideOut out, bool cull,
+              CrowdList crowd, unsigned *status) {
+  __shared__ float4 sPos[kCrowdWarps][32];
+  __shared__ float4 sVel[kCrowdWarps][32];
+  __shared__ unsigned char sQ[kCrowdWarps][32][32];  // [warp][entry][lane]
+  const SimParams &P = kp.p;
+  const unsigned total = min(__ldg(crowd.count), crowd.cap);
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const unsigned warps = gridDim.x * kCrowdWarps;
+  unsigned k = blockIdx.x * kCrowdWarps + warp;
+  const float inf = __int_as_float(0x7f800000);
+  float4 *cPos = sPos[warp];
+  float4 *cVel = sVel[warp];
+  unsigned char *q = &sQ[warp][0][lane];
+  while (k < total) {
+    const uint2 gr = crowd.groups[k];
+    const unsigned i = gr.x + lane;
+    bool valid = lane < gr.y && i < n;
+    const float4 p4 = ldg4(sortedPos + (valid ? i : gr.x));
+    const float4 v4 = ldg4(sortedVel + (valid ? i : gr.x));
+    const float3 pos = make_float3(p4.x, p4.y, p4.z), vel = make_float3(v4.x, v4.y, v4.z);
+    const float ri = kRadiusFromW ? p4.w : P.particleRadius;
+    const int3 g = gridPos(pos.x, pos.y, pos.z, P);
+    // the group's cell is its first member's; a member hashed elsewhere was
+    // not deferred (kCollideGlobal kept it)
+    const int gx = __shfl_sync(0xffffffffu, g.x, 0), gy = __shfl_sync(0xffffffffu, g.y, 0),
+              gz = __shfl_sync(0xffffffffu, g.z, 0);
+    valid = valid && gridHash(g.x, g.y, g.z, P) == gridHash(gx, gy, gz, P);
+    bool lcull = cull;
+    if (valid && kRadiusFromW && !(ri <= P.particleRadius)) {
+      atomicOr(status, (unsigned)kStatusRadiusBound);
+      lcull = false;
+    }
+    const CellCull cc = makeCull(pos, g, ri + P.particleRadius, P);
+    const float cullR2 = lcull ? cc.r2 : inf;
+    const float cdMono = ri + P.particleRadius;
+    const float cdMonoHi2 = rejectBound(cdMono);
+    float3 force = make_float3(0.0f, 0.0f, 0.0f);
+#pragma unroll 1
+    for (int c27 = 0; c27 < 27; c27++) {
+      const int z = c27 / 9 - 1, y = (c27 / 3) % 3 - 1, x = c27 % 3 - 1;
+      const float boxD2 = CellCull::pick(z, cc.zl, cc.zh) + CellCull::pick(y, cc.yl, cc.yh) +
+                          CellCull::pick(x, cc.xl, cc.xh);
+      if (__all_sync(0xffffffffu, !valid || boxD2 > cullR2)) continue;
+      unsigned a, b;
+      cellRange<kPrefix>(gridHash(gx + x, gy + y, gz + z, P), cells, n, a, b);
+      if (a >= b) continue;
+      float3 cf = make_float3(0.0f, 0.0f, 0.0f);
+      float4 nP = make_float4(0.0f, 0.0f, 0.0f, 0.0f), nV = nP;
+      if (a + lane < b) {
+        nP = ldg4(sortedPos + a + lane);
+        nV = ldg4(sortedVel + a + lane);
+      }
+#pragma unroll 1
+      for (unsigned j0 = a; j0 < b; j0 += 32) {
+        const unsigned cnt = min(32u, b - j0);
+        __syncwarp();  // the previous chunk is no longer read
+        cPos[lane] = nP;
+        cVel[lane] = nV;
+        const unsigned jn = j0 + 32 + lane;
+        if (jn < b) {  // prefetch the next chunk
+          nP = ldg4(sortedPos + jn);
+          nV = ldg4(sortedVel + jn);
+        }
+        __syncwarp();
+        // scan: squared-distance test, near partners queued in order
+        int qn = 0;
+#pragma unroll 4
+        for (unsigned t = 0; t < cnt; ++t) {
+          const float4 q4 = cPos[t];
+          const float3 rel = make_float3(q4.x - pos.x, q4.y - pos.y, q4.z - pos.z);
+          const float d2 = pairDist2(rel);
+          const float hi2 = kRadiusFromW ? rejectBound(ri + q4.w) : cdMonoHi2;
+          if (valid && d2 < hi2 && j0 + t != i) {
+            q[qn * 32] = (unsigned char)t;
+            ++qn;
+          }
+        }
+        // drain: exact test and terms, in queue (= partner) order
+        const int m = __reduce_max_sync(0xffffffffu, (unsigned)qn);
+        for (int e = 0; e < m; ++e) {
+          if (e < qn) {
+            const unsigned t = q[e * 32];
+            const float4 q4 = cPos[t];
+            const float3 rel = make_float3(q4.x - pos.x, q4.y - pos.y, q4.z - pos.z);
+            const float dist = sqrtf(pairDist2(rel));
+            const float cd = kRadiusFromW ? ri + q4.w : cdMono;
+            if (dist < cd) {
+              const float4 w4 = cVel[t];
+              const float3 f = contactTerm(rel, dist, cd, vel, make_float3(w4.x, w4.y, w4.z),
+                                           P.attraction, P);
+              cf.x = cf.x + f.x;
+              cf.y = cf.y + f.y;
+              cf.z = cf.z + f.z;
+            }
+          }
+        }
+      }
+      force.x = force.x + cf.x;
+      force.y = force.y + cf.y;
+      force.z = force.z + cf.z;
+    }
+    if (valid)
+      finishParticle<kMode, kCollider, kForceOut>(i, n, pos, vel, p4, ri, force, index, newVel,
+                                                  out, P);
+    unsigned next = 0;
+    if (lane == 0) next = warps + atomicAdd(crowd.count + 1, 1u);
+    k = __shfl_sync(0xffffffffu, next, 0);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -534,6 +742,36 @@ kCollideTiled(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
                                                 out, P);
 }
 
+bool g_crowdPath = true;  // fcdemSetCrowdPath
+unsigned g_crowdLimit = kCrowdLimit;  // fcdemSetCrowdLimit
+constexpr unsigned kCrowdCtas = 152 * 4;
+
+// The group list for n particles (grown on demand; at most one group per
+// particle), its counters cleared on the current stream.  groups == nullptr
+// when the path is off or the list cannot be had.
+CrowdList crowdList(unsigned n) {
+  CrowdList cl{nullptr, nullptr, 0u, g_crowdLimit};
+  if (!g_crowdPath) return cl;
+  Context &c = ctx();
+  if (c.crowdBuf == nullptr || c.crowdCap < n) {
+    if (!cudaOk(cudaDeviceSynchronize())) return cl;
+    if (c.crowdBuf) cudaFree(c.crowdBuf);
+    c.crowdBuf = nullptr;
+    c.crowdCap = 0;
+    if (cudaMalloc(&c.crowdBuf, 16 + 8 * (size_t)n) != cudaSuccess) {
+      cudaGetLastError();
+      c.crowdBuf = nullptr;
+      return cl;  // the plain path covers every particle
+    }
+    c.crowdCap = n;
+  }
+  if (!cudaOk(cudaMemsetAsync(c.crowdBuf, 0, 8, curStream()))) return cl;
+  cl.count = (unsigned *)c.crowdBuf;
+  cl.groups = (uint2 *)((char *)c.crowdBuf + 16);
+  cl.cap = n;
+  return cl;
+}
+
 template <int kMode, bool kRadiusFromW, bool kCollider, bool kForceOut, bool kPrefix>
 void launchT(bool tiled, bool cull, unsigned n, float4 *newVel, const float4 *sp,
              const float4 *sv, const unsigned *index, const CellRanges &cells,
@@ -543,10 +781,17 @@ void launchT(bool tiled, bool cull, unsigned n, float4 *newVel, const float4 *sp
     kCollideTiled<kMode, kRadiusFromW, kCollider, kForceOut>
         <<<blocks, kTileThreads, 0, curStream()>>>(newVel, sp, sv, index, cells, n, kp, out,
                                                    ctx().dStatus);
-  else
+  else {
+    const CrowdList crowd = crowdList(n);
     kCollideGlobal<kMode, kRadiusFromW, kCollider, kForceOut, kPrefix>
         <<<blocks, 128, 0, curStream()>>>(newVel, sp, sv, index, cells, n, kp, out, cull,
-                                          ctx().dStatus);
+                                          crowd, ctx().dStatus);
+    if (crowd.groups && launchOk())
+      kCollideCrowd<kMode, kRadiusFromW, kCollider, kForceOut, kPrefix>
+          <<<kCrowdCtas, kCrowdWarps * 32, 0, curStream()>>>(newVel, sp, sv, index, cells, n,
+                                                             kp, out, cull, crowd,
+                                                             ctx().dStatus);
+  }
 }
 
 // Batched collide (fcdem_batch.cu): slot i belongs to scene sceneOf[i]; its
@@ -688,3 +933,9 @@ extern "C" void fcdemSetCollidePath(int path) {
 }
 
 extern "C" void fcdemSetCellCulling(int on) { fcdem::g_cullCells = on != 0; }
+
+extern "C" void fcdemSetCrowdPath(int on) { fcdem::g_crowdPath = on != 0; }
+
+extern "C" void fcdemSetCrowdLimit(unsigned limit) {
+  fcdem::g_crowdLimit = limit ? limit : fcdem::kCrowdLimit;
+}

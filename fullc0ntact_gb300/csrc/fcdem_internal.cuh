@@ -54,6 +54,8 @@ struct Context {
   void *countBuf = nullptr;     // counting-sort pipeline of fcdemUpdate
   size_t countBytes = 0;
   unsigned countCells = 0;
+  void *crowdBuf = nullptr;     // collide: groups of crowded particles
+  unsigned crowdCap = 0;        // particles the group list covers
 };
 
 // The context of the calling thread's current device (created on first use).

@@ -179,6 +179,16 @@ void fcdemSetRadiusMode(int radiusFromW);
  * either way; the switch exists to measure and test that. */
 void fcdemSetCellCulling(int on);
 
+/* Crowded-neighbourhood path in collide (default on): particles whose 27
+ * neighbour cells hold more than a limit (fcdemSetCrowdLimit) are computed
+ * by a second kernel, one warp per group of up to 32 members of a cell.
+ * Results are identical either way; the switch exists to measure and test
+ * that. */
+void fcdemSetCrowdPath(int on);
+/* Neighbourhood size above which the crowded path takes a particle
+ * (0: the default, 1024). */
+void fcdemSetCrowdLimit(uint limit);
+
 /* Library version string. */
 const char *fcdemVersion(void);
 
