@@ -23,6 +23,7 @@ SOURCES = [
     "fcdem_count.cu",
     "fcdem_distmap.cu",
     "fcdem_batch.cu",
+    "fcdem_sdf.cu",
     "fcdem_host.cpp",
 ]
 

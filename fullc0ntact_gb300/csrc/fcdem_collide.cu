@@ -900,6 +900,11 @@ void launchCollide(int mode, bool collider, float4 *newVel, const float4 *sp,
   FCDEM_COLLIDE_CASE(2, true, true, false, true)
   FCDEM_COLLIDE_CASE(3, false, true, false, true)
   FCDEM_COLLIDE_CASE(3, true, true, false, true)
+  // fcdemUM_update: evalForces (no collider, optional force) on the prefix table
+  FCDEM_COLLIDE_CASE(0, false, false, false, true)
+  FCDEM_COLLIDE_CASE(0, true, false, false, true)
+  FCDEM_COLLIDE_CASE(0, false, false, true, true)
+  FCDEM_COLLIDE_CASE(0, true, false, true, true)
 #undef FCDEM_COLLIDE_CASE
   setError(FCDEM_ERR_INVALID_VALUE);
 }

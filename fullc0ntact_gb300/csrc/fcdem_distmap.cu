@@ -1,165 +1,52 @@
 // fcdem_distmap.cu -- distance-map boundary (inshape3dcore/grid/distancemap.*,
 // cuda_addon/distancemap.cuh:118-302, cuda_addon/boundaries.cuh:38-89) and
 // the particledem_um entry points that use it (cuda_addon/particledem_um.cu).
-//
-// Map layout on the device: one float4 per lattice vertex, (distance, contact
-// point x, y, z), vertex (i, j, k) at k*(cx+1)*(cy+1) + j*(cx+1) + i -- the
-// reference keeps distance_ and contactPoints_ in separate arrays and the
-// vertex coordinates in a third; here a corner is one 16-byte load and the
-// coordinates are recomputed exactly as the host built them
-// (vmin + i*cellSize in float, distancemap.cpp:214-226).
+// The map types and the query live in fcdem_map.cuh.
 #include <cmath>
 #include <cstdlib>
 
-#include "fcdem_dem.cuh"
-
-struct fcdemDistanceMap {
-  float vmin[3], vmax[3];
-  float cellSize;
-  int cells[3];
-  float4 *vert;  // device
-  int device;
-};
+#include "fcdem_map.cuh"
 
 namespace fcdem {
 namespace {
 
-struct MapView {
-  float3 vmin, vmax;
-  float cellSize;
-  float invCell;  // (float)(1.0 / cellSize), as distancemap.cuh:173-174
-  int cells[3];
-  const float4 *__restrict__ vert;
-};
-
-MapView view(const fcdemDistanceMap *m) {
-  MapView v;
-  v.vmin = make_float3(m->vmin[0], m->vmin[1], m->vmin[2]);
-  v.vmax = make_float3(m->vmax[0], m->vmax[1], m->vmax[2]);
-  v.cellSize = m->cellSize;
-  v.invCell = (float)(1.0 / (double)m->cellSize);
-  for (int k = 0; k < 3; ++k) v.cells[k] = m->cells[k];
-  v.vert = m->vert;
-  return v;
-}
-
-// vmin + i * cellSize with two roundings, as the host lattice (no fused
-// multiply-add: the reference computed it on the CPU).
-__device__ __forceinline__ float vcoord(float vmin, int i, float cs) {
-  return __fadd_rn(vmin, __fmul_rn((float)i, cs));
-}
-
-// DistanceMap<float,gpu>::queryMap (distancemap.cuh:154-191).  Returns the
-// trilinear distance (5.0 outside the box) and contact point.  The cell index
-// is clamped to cells-1 (the reference reads one vertex past the row for a
-// query on the upper face).
-__device__ __forceinline__ float queryMap(const MapView &M, float3 q, float3 &cp) {
-  if (!(M.vmin.x <= q.x && q.x <= M.vmax.x && M.vmin.y <= q.y && q.y <= M.vmax.y &&
-        M.vmin.z <= q.z && q.z <= M.vmax.z))
-    return 5.0f;
-  int x = (int)(fabsf(q.x - M.vmin.x) * M.invCell);
-  int y = (int)(fabsf(q.y - M.vmin.y) * M.invCell);
-  int z = (int)(fabsf(q.z - M.vmin.z) * M.invCell);
-  x = min(max(x, 0), M.cells[0] - 1);
-  y = min(max(y, 0), M.cells[1] - 1);
-  z = min(max(z, 0), M.cells[2] - 1);
-  // vertexIndices (distancemap.cuh:281-302)
-  const int ix = M.cells[0] + 1;
-  const int islice = (M.cells[0] + 1) * (M.cells[1] + 1);
-  const int b = z * islice + y * ix + x;
-  const float4 c0 = __ldg(M.vert + b), c1 = __ldg(M.vert + b + 1);
-  const float4 c2 = __ldg(M.vert + b + ix + 1), c3 = __ldg(M.vert + b + ix);
-  const float4 c4 = __ldg(M.vert + b + islice), c5 = __ldg(M.vert + b + islice + 1);
-  const float4 c6 = __ldg(M.vert + b + ix + islice + 1), c7 = __ldg(M.vert + b + ix + islice);
-  const float x0 = vcoord(M.vmin.x, x, M.cellSize), x1 = vcoord(M.vmin.x, x + 1, M.cellSize);
-  const float y0 = vcoord(M.vmin.y, y, M.cellSize), y1 = vcoord(M.vmin.y, y + 1, M.cellSize);
-  const float z0 = vcoord(M.vmin.z, z, M.cellSize), z1 = vcoord(M.vmin.z, z + 1, M.cellSize);
-  const float xd = (q.x - x0) / (x1 - x0);
-  const float yd = (q.y - y0) / (y1 - y0);
-  const float zd = (q.z - z0) / (z1 - z0);
-  // trilinearInterpolateDistance (distancemap.cuh:227-252).  In
-  // `d0 * (1.0 - x_d) + d1 * x_d` the first product is double (1.0 is a
-  // double literal), the second float * float; the sum is double, rounded to
-  // float on assignment.  __fmul_rn keeps the float product unfused.
-  const double wx = 1.0 - (double)xd, wy = 1.0 - (double)yd, wz = 1.0 - (double)zd;
-  const float d00 = (float)((double)c0.x * wx + (double)__fmul_rn(c1.x, xd));
-  const float d10 = (float)((double)c3.x * wx + (double)__fmul_rn(c2.x, xd));
-  const float d01 = (float)((double)c4.x * wx + (double)__fmul_rn(c5.x, xd));
-  const float d11 = (float)((double)c7.x * wx + (double)__fmul_rn(c6.x, xd));
-  const float d0 = (float)((double)d00 * wy + (double)__fmul_rn(d10, yd));
-  const float d1 = (float)((double)d01 * wy + (double)__fmul_rn(d11, yd));
-  const float dist = (float)((double)d0 * wz + (double)__fmul_rn(d1, zd));
-  // trilinearInterpolateCP (distancemap.cuh:254-279): Vector3<float> times the
-  // weight converted to float
-  const float fwx = (float)wx, fwy = (float)wy, fwz = (float)wz;
-  float3 a00 = make_float3(c0.y * fwx + c1.y * xd, c0.z * fwx + c1.z * xd, c0.w * fwx + c1.w * xd);
-  float3 a10 = make_float3(c3.y * fwx + c2.y * xd, c3.z * fwx + c2.z * xd, c3.w * fwx + c2.w * xd);
-  float3 a01 = make_float3(c4.y * fwx + c5.y * xd, c4.z * fwx + c5.z * xd, c4.w * fwx + c5.w * xd);
-  float3 a11 = make_float3(c7.y * fwx + c6.y * xd, c7.z * fwx + c6.z * xd, c7.w * fwx + c6.w * xd);
-  float3 a0 = make_float3(a00.x * fwy + a10.x * yd, a00.y * fwy + a10.y * yd, a00.z * fwy + a10.z * yd);
-  float3 a1 = make_float3(a01.x * fwy + a11.x * yd, a01.y * fwy + a11.y * yd, a01.z * fwy + a11.z * yd);
-  cp = make_float3(a0.x * fwz + a1.x * zd, a0.y * fwz + a1.y * zd, a0.z * fwz + a1.z * zd);
-  return dist;
-}
-
-// checkDistMap (boundaries.cuh:38-63)
-__device__ __forceinline__ void checkDistMap(const MapView &M, float radius, float bd,
-                                             float3 &pos, float3 &vel) {
-  float3 cp = make_float3(0.0f, 0.0f, 0.0f);
-  const float dist = queryMap(M, pos, cp);
-  if (dist < radius) {
-    float3 n0 = make_float3(pos.x - cp.x, pos.y - cp.y, pos.z - cp.z);
-    float invLen = rsqrtf(n0.x * n0.x + n0.y * n0.y + n0.z * n0.z);
-    float3 n = make_float3(n0.x * invLen, n0.y * invLen, n0.z * invLen);
-    float pen = radius - dist;
-    float extra = (float)(0.1 * (double)radius);
-    pos = make_float3(pos.x + n.x * pen, pos.y + n.y * pen, pos.z + n.z * pen);
-    pos = make_float3(pos.x + n.x * extra, pos.y + n.y * extra, pos.z + n.z * extra);
-    vel.x = vel.x * (0.5f * bd);
-    vel.y = vel.y * (0.5f * bd);
-    vel.z = vel.z * (0.7f * bd);
-  }
-}
-
 // d_integrateSystem + d_checkBoundaryDistMap (particledem_um.cu:604-638,
 // boundaries.cuh:65-89): integrate, map contact, r = 1 cylinder around z,
 // z planes at -1 and 10.  vel.w receives pos.w (particledem_um.cu:636).
+// kCount: also the next step's calcHash and cell count (counting pipeline).
+template <bool kCount>
 __global__ void __launch_bounds__(256)
 kIntegrateDistMap(float4 *__restrict__ pos, float4 *__restrict__ vel, float dt, unsigned n,
-                  KParams kp, MapView M, int useMap) {
+                  KParams kp, MapView M, int useMap, UmCount count) {
   unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const SimParams &P = kp.p;
   float4 p4 = pos[i], v4 = vel[i];
   float3 p = make_float3(p4.x, p4.y, p4.z), v = make_float3(v4.x, v4.y, v4.z);
   const float r = kp.radiusFromW ? p4.w : P.particleRadius;
-  const float bd = P.boundaryDamping;
-  v.x = v.x + P.gravity[0] * dt;
-  v.y = v.y + P.gravity[1] * dt;
-  v.z = v.z + P.gravity[2] * dt;
-  v.x = v.x * P.globalDamping;
-  v.y = v.y * P.globalDamping;
-  v.z = v.z * P.globalDamping;
-  p.x = p.x + v.x * dt;
-  p.y = p.y + v.y * dt;
-  p.z = p.z + v.z * dt;
-  // the cylinder test uses the position before the map push
-  const float px0 = p.x, py0 = p.y;
-  const float len = sqrtf(px0 * px0 + py0 * py0 + 0.0f * 0.0f);
-  if (useMap) checkDistMap(M, r, bd, p, v);
-  if (len > 1.0f) {
-    float pen = len - 1.0f;
-    float invLen = rsqrtf(px0 * px0 + py0 * py0 + 0.0f * 0.0f);
-    float3 nn = make_float3(px0 * invLen, py0 * invLen, 0.0f * invLen);
-    float s = pen + r;
-    p = make_float3(p.x - nn.x * s, p.y - nn.y * s, p.z - nn.z * s);
-    v.x = v.x * bd;
-    v.y = v.y * bd;
-  }
-  if (p.z > 10.0f - r) { p.z = 10.0f - r; v.z = v.z * bd; }
-  if (p.z < -1.0f + r) { p.z = -1.0f + r; v.z = v.z * bd; }
+  umAdvance(p, v, dt, P);
+  umBoundary(M, useMap != 0, r, P.boundaryDamping, p, v);
   pos[i] = make_float4(p.x, p.y, p.z, p4.w);
   vel[i] = make_float4(v.x, v.y, v.z, p4.w);
+  if (kCount) {
+    const int3 gp = gridPos(p.x, p.y, p.z, P);
+    const unsigned h = gridHash(gp.x, gp.y, gp.z, P);
+    count.hash[i] = h;
+    count.rank[i] = atomicAdd(count.cnt + h, 1u);
+    countTile(count.tileCnt, h >> 12);
+  }
+}
+
+__global__ void __launch_bounds__(256)
+kHashCount(const float4 *__restrict__ pos, unsigned n, KParams kp, UmCount count) {
+  unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 p4 = __ldg(pos + i);
+  const int3 gp = gridPos(p4.x, p4.y, p4.z, kp.p);
+  const unsigned h = gridHash(gp.x, gp.y, gp.z, kp.p);
+  count.hash[i] = h;
+  count.rank[i] = atomicAdd(count.cnt + h, 1u);
+  countTile(count.tileCnt, h >> 12);
 }
 
 __global__ void __launch_bounds__(256)
@@ -204,6 +91,29 @@ kTorusMap(float4 *__restrict__ vert, int vx, int vy, int vz, float3 vmin, float 
 }
 
 }  // namespace
+}  // namespace fcdem
+
+namespace fcdem {
+
+bool umHashCount(const float4 *pos, unsigned n, const KParams &kp, const UmCount &count) {
+  kHashCount<<<(n + 255) / 256, 256, 0, curStream()>>>(pos, n, kp, count);
+  return launchOk();
+}
+
+bool mapIntegrate(float4 *pos, float4 *vel, float dt, unsigned n, const KParams &kp,
+                  const fcdemDistanceMap *map, const UmCount *count) {
+  MapView M{};
+  if (map) M = view(map);
+  const unsigned blocks = (n + 255) / 256;
+  if (count)
+    kIntegrateDistMap<true><<<blocks, 256, 0, curStream()>>>(pos, vel, dt, n, kp, M,
+                                                             map ? 1 : 0, *count);
+  else
+    kIntegrateDistMap<false><<<blocks, 256, 0, curStream()>>>(pos, vel, dt, n, kp, M,
+                                                              map ? 1 : 0, UmCount{});
+  return launchOk();
+}
+
 }  // namespace fcdem
 
 using namespace fcdem;
@@ -316,11 +226,7 @@ void fcdemUM_integrateSystem(float *pos, float *vel, float deltaTime, uint numPa
   if (!c.haveParams) { setError(FCDEM_ERR_NO_PARAMS); return; }
   if (numParticles == 0) return;
   if (!pos || !vel) { setError(FCDEM_ERR_INVALID_VALUE); return; }
-  MapView M{};
-  if (map) M = view(map);
-  kIntegrateDistMap<<<(numParticles + 255) / 256, 256, 0, curStream()>>>(
-      (float4 *)pos, (float4 *)vel, deltaTime, numParticles, kparams(c), M, map ? 1 : 0);
-  launchOk();
+  mapIntegrate((float4 *)pos, (float4 *)vel, deltaTime, numParticles, kparams(c), map, nullptr);
 }
 
 void fcdemUM_evalForces(float *newVel, float *force, float *sortedPos, float *sortedVel,

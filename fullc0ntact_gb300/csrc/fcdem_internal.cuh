@@ -175,4 +175,22 @@ bool countPipelineSort(Context &c, const CountBuffers &b, const unsigned *origOf
 bool countPipelineTables(const CountBuffers &b, unsigned *cellStart, unsigned *cellEnd,
                          unsigned numCells);
 
+
+// Unified-memory (particledem_um) step on the counting pipeline: the
+// integrate with the distance-map boundary also writes the next step's
+// calcHash and cell count (UmCount; nullptr on the last step).
+struct UmCount {
+  unsigned *hash, *rank, *cnt, *tileCnt;
+};
+// calcHash + count of the current positions (the first step).
+bool umHashCount(const float4 *pos, unsigned n, const KParams &kp, const UmCount &count);
+// d_integrateSystem + d_checkBoundaryDistMap, exact map query (map may be
+// nullptr: no obstacle).
+bool mapIntegrate(float4 *pos, float4 *vel, float dt, unsigned n, const KParams &kp,
+                  const fcdemDistanceMap *map, const UmCount *count);
+// The same with the neural-SDF culling of the map query (fcdem_sdf.cu).
+bool sdfIntegrate(fcdemSdfNet *net, float4 *pos, float4 *vel, float dt, unsigned n,
+                  const KParams &kp, const fcdemDistanceMap *map, float skin, unsigned *exact,
+                  const UmCount *count);
+
 }  // namespace fcdem

@@ -341,4 +341,60 @@ void fcdemUpdate(float *pos, float *vel, float *sortedPos, float *sortedVel,
 
 void fcdemSetUpdatePipeline(int pipeline) { g_updatePipeline = pipeline == 0 ? 0 : 1; }
 
+void fcdemUM_update(float *pos, float *vel, float *force, float *sortedPos, float *sortedVel,
+                    uint *hash, uint *index, uint *cellStart, uint *cellEnd, float deltaTime,
+                    uint numParticles, uint numCells, uint steps, const fcdemDistanceMap *map,
+                    fcdemSdfNet *net, float skin, uint *exactQueries) {
+  Context &c = ctx();
+  if (!readyFor(c) || !tablesOk(c.params, numCells)) return;
+  if (steps == 0 || numParticles == 0) return;
+  if (!pos || !vel || !sortedPos || !sortedVel || !hash || !index || !cellStart || !cellEnd ||
+      numCells == 0 || (net && (!map || !(skin >= 0.0f)))) {
+    setError(FCDEM_ERR_INVALID_VALUE);
+    return;
+  }
+  const KParams kp = kparams(c);
+  const unsigned n = numParticles;
+  // Per step, as CollisionPipeline<dem_gpu_unified>::startPipeline
+  // (dempipeline.hpp:113-120): calcHash, sortParticles, reorder, evalForces,
+  // integrateSystem.  The sort is the counting pipeline from particle order
+  // each step; evalForces writes vel (and force) in particle order; the
+  // integrate also writes the next step's hash and count.
+  CountBuffers b;
+  if (!countBuffersIn(c.countBuf, c.countBytes, c.countCells, n, numCells, b)) return;
+  const UmCount count{hash, b.rank, b.cnt, b.tileCnt};
+  stageBegin(0);
+  bool ok = umHashCount((const float4 *)pos, n, kp, count);
+  stageEnd(0);
+  for (uint s = 0; ok && s < steps; ++s) {
+    stageBegin(1);
+    ok = countPipelineSort(c, b, nullptr, (const float4 *)pos, (const float4 *)vel, hash, index,
+                           (float4 *)sortedPos, (float4 *)sortedVel, n, numCells);
+    stageEnd(1);
+    if (!ok) break;
+    CellRanges cells;
+    cells.off = b.off;
+    CollideOut out;
+    out.force = (float3 *)force;
+    stageBegin(4);
+    launchCollide(0, false, (float4 *)vel, (const float4 *)sortedPos, (const float4 *)sortedVel,
+                  index, cells, n, kp, out);
+    stageEnd(4);
+    const bool last = (s + 1 == steps);
+    stageBegin(0);
+    if (net)
+      ok = sdfIntegrate(net, (float4 *)pos, (float4 *)vel, deltaTime, n, kp, map, skin,
+                        exactQueries, last ? nullptr : &count);
+    else
+      ok = mapIntegrate((float4 *)pos, (float4 *)vel, deltaTime, n, kp, map,
+                        last ? nullptr : &count);
+    stageEnd(0);
+  }
+  if (ok) {
+    stageBegin(2);
+    countPipelineTables(b, cellStart, cellEnd, numCells);
+    stageEnd(2);
+  }
+}
+
 }  // extern "C"

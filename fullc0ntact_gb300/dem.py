@@ -301,6 +301,51 @@ def um_reorder(cell_start, cell_end, sorted_pos, sorted_vel, hash_, index, old_p
                                             _p(old_vel), n, num_cells)
 
 
+lib.fcdemUM_update.argtypes = [C.c_void_p] * 9 + [C.c_float, C.c_uint, C.c_uint, C.c_uint,
+                                                  C.c_void_p, C.c_void_p, C.c_float,
+                                                  C.c_void_p]
+lib.fcdemUM_update.restype = None
+
+
+class UmScene(DeviceScene):
+    """A scene on the unified-memory DEM path (particledem_um.cu): the
+    ParticleWorld arrays plus force_, the distance-map obstacle, and the step
+    of CollisionPipeline<dem_gpu_unified> (dempipeline.hpp:113-120)."""
+
+    def __init__(self, scene: dict, dmap: DistanceMap | None = None,
+                 device: str | torch.device = "cuda"):
+        super().__init__(scene, device)
+        self.dmap = dmap
+        self.force = torch.zeros((self.n, 3), dtype=torch.float32, device=self.pos.device)
+
+    def stages(self, dt: float | None = None) -> None:
+        """One step as the reference issues it: calcHash, sortParticles,
+        reorderDataAndFindCellStart, evalForces, integrateSystem."""
+        dt = self.dt if dt is None else dt
+        self.activate()
+        calc_hash(self.hash, self.index, self.pos, self.n)
+        sort_particles(self.hash, self.index, self.n)
+        um_reorder(self.cell_start, self.cell_end, self.sorted_pos, self.sorted_vel, self.hash,
+                   self.index, self.pos, self.vel, self.n, self.num_cells)
+        um_eval_forces(self.vel, self.force, self.sorted_pos, self.sorted_vel, self.index,
+                       self.cell_start, self.cell_end, self.n, self.num_cells)
+        um_integrate_system(self.pos, self.vel, dt, self.n, self.dmap)
+
+    def update(self, steps: int = 1, dt: float | None = None, net=None, skin: float = 0.0,
+               exact_counter: torch.Tensor | None = None, force: bool = True) -> None:
+        """`steps` steps through the fused fcdemUM_update; with `net` (an
+        sdf.SdfNet) the map query is culled where the network predicts a
+        distance above `skin`."""
+        dt = self.dt if dt is None else dt
+        self.activate()
+        lib.fcdemUM_update(_p(self.pos), _p(self.vel), _p(self.force) if force else None,
+                           _p(self.sorted_pos), _p(self.sorted_vel), _p(self.hash),
+                           _p(self.index), _p(self.cell_start), _p(self.cell_end), dt, self.n,
+                           self.num_cells, steps, self.dmap.handle if self.dmap else None,
+                           net.handle if net is not None else None, skin,
+                           _p(exact_counter) if exact_counter is not None else None)
+
+
 # --- batches of scenes --------------------------------------------------------
 
 class _BatchScene(C.Structure):

@@ -86,6 +86,35 @@ def config1(n: int = 4194304, seed: int = 2024, grid: int = 256,
                 radius_from_w=True, dt=0.5, box_side=side)
 
 
+def config2(n: int = 1048576, seed: int = 2, grid: int = 256, z0: float = 0.15) -> dict:
+    """Spheres falling onto a torus (the distance-map obstacle): n spheres of
+    radius 1/256 on a jittered lattice (spacing 2.2 r, jitter 0.05 r),
+    128 x 128 columns wide, centred over the torus (R 0.3, r 0.1, in the
+    z = 0 plane) and starting at z = z0; velocities U[-0.001, 0.001];
+    gravity -3e-4 along z, the config0 contact parameters, dt 0.5; grid^3
+    cells of one diameter from (-1, -1, -1); no collider sphere (the
+    unified-memory evalForces has none)."""
+    r = 1.0 / 256.0
+    sp = 2.2 * r
+    nx = ny = 128 if n >= 128 * 128 else max(1, int(np.sqrt(n)))
+    nz = (n + nx * ny - 1) // (nx * ny)
+    rng = np.random.default_rng(seed)
+    k = np.arange(n)
+    ix, iy, iz = k % nx, (k // nx) % ny, k // (nx * ny)
+    pos = np.zeros((n, 4), np.float32)
+    pos[:, 0] = (ix - (nx - 1) / 2.0) * sp
+    pos[:, 1] = (iy - (ny - 1) / 2.0) * sp
+    pos[:, 2] = z0 + iz * sp
+    pos[:, :3] += rng.uniform(-0.05 * r, 0.05 * r, (n, 3))
+    pos[:, 3] = 1.0
+    vel = np.zeros((n, 4), np.float32)
+    vel[:, :3] = rng.uniform(-0.001, 0.001, (n, 3))
+    p = make_params(n, (grid, grid, grid), r, gravity=(0.0, 0.0, -3e-4),
+                    collider_pos=(10.0, 10.0, 10.0), collider_radius=0.0)
+    return dict(name=f"torus-{n}", pos=pos, vel=vel, params=p, radius_from_w=False, dt=0.5,
+                radius=r)
+
+
 def random_box(n: int, grid=(16, 16, 16), radius: float = 1.0 / 16.0, seed: int = 7,
                vel_range: float = 0.01, cell: float | None = None,
                origin=(-1.0, -1.0, -1.0), poly: bool = False) -> dict:

@@ -1,0 +1,147 @@
+"""Neural signed-distance field of an obstacle (the C-ABI's fcdemSdf* calls).
+
+``SdfNet`` wraps one network: FP32 master parameters on the device, trained
+by the library's own forward/backward kernels and Adam on samples of a
+``DistanceMap``; BF16 tensor-core inference; the culled boundary integrate
+(``um_integrate_system_sdf``), whose results equal ``dem.um_integrate_system``
+while the network's error stays below the skin band.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from ._native import check, lib
+from .dem import DistanceMap, _p
+
+vp = C.c_void_p
+u32 = C.c_uint
+f32 = C.c_float
+_F3 = C.c_float * 3
+
+_SIGS = {
+    "fcdemSdfCreate": (vp, [C.c_int, C.c_int, C.c_int, C.c_ulonglong]),
+    "fcdemSdfDestroy": (None, [vp]),
+    "fcdemSdfNumParams": (u32, [vp]),
+    "fcdemSdfGetParams": (None, [vp, vp]),
+    "fcdemSdfSetParams": (None, [vp, vp]),
+    "fcdemSdfSetNormalization": (None, [vp, _F3, _F3, f32]),
+    "fcdemSdfGetNormalization": (None, [vp, _F3, _F3, C.POINTER(f32)]),
+    "fcdemSdfSamples": (None, [vp, C.c_int, u32, f32, f32, C.c_ulonglong, vp, vp]),
+    "fcdemSdfGradient": (f32, [vp, vp, vp, u32, f32, vp]),
+    "fcdemSdfTrainSamples": (f32, [vp, vp, vp, u32, u32, u32, f32, f32]),
+    "fcdemSdfEvalF32": (None, [vp, vp, vp, u32, vp]),
+    "fcdemSdfInfer": (None, [vp, vp, vp, u32, vp]),
+    "fcdemUM_integrateSystemSdf": (None, [vp, vp, f32, u32, vp, vp, f32, vp]),
+}
+for _name, (_res, _args) in _SIGS.items():
+    _f = getattr(lib, _name)
+    _f.restype = _res
+    _f.argtypes = _args
+
+
+def _opt(t: torch.Tensor | None):
+    return None if t is None else _p(t)
+
+
+class SdfNet:
+    """inputs = 3 + number of shape codes; hidden 64 or 128; 2 or 3 hidden
+    layers (3 -> 64 -> 64 -> 64 -> 1 is SdfNet(3, 64, 3))."""
+
+    def __init__(self, inputs: int = 3, hidden: int = 64, layers: int = 3, seed: int = 1):
+        self.inputs, self.hidden, self.layers = inputs, hidden, layers
+        h = lib.fcdemSdfCreate(inputs, hidden, layers, seed)
+        check("fcdemSdfCreate")
+        if not h:
+            raise MemoryError("fcdemSdfCreate failed")
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def num_params(self) -> int:
+        return int(lib.fcdemSdfNumParams(self._h))
+
+    def get_params(self) -> np.ndarray:
+        out = np.zeros(self.num_params, np.float32)
+        lib.fcdemSdfGetParams(self._h, out.ctypes.data)
+        check("fcdemSdfGetParams")
+        return out
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.shape == (self.num_params,)
+        lib.fcdemSdfSetParams(self._h, p.ctypes.data)
+        check("fcdemSdfSetParams")
+
+    def set_normalization(self, shift, scale, out_scale: float) -> None:
+        lib.fcdemSdfSetNormalization(self._h, _F3(*map(float, shift)), _F3(*map(float, scale)),
+                                     float(out_scale))
+        check("fcdemSdfSetNormalization")
+
+    def normalization(self):
+        s, c, o = _F3(), _F3(), f32()
+        lib.fcdemSdfGetNormalization(self._h, s, c, C.byref(o))
+        return np.array(s, np.float32), np.array(c, np.float32), float(o.value)
+
+    def normalize_to(self, dmap: DistanceMap) -> None:
+        """Inputs scaled to [-1, 1] over the map box (one scale for all axes),
+        outputs in units of the box's largest half-extent."""
+        centre = 0.5 * (dmap.vmin + dmap.vmax)
+        half = float(np.max(0.5 * (dmap.vmax - dmap.vmin)))
+        self.set_normalization(centre, [1.0 / half] * 3, half)
+
+    def gradient(self, samples: torch.Tensor, shapes: torch.Tensor | None = None,
+                 band: float = 0.0):
+        g = np.zeros(self.num_params, np.float32)
+        loss = lib.fcdemSdfGradient(self._h, _p(samples), _opt(shapes), samples.shape[0],
+                                    band, g.ctypes.data)
+        check("fcdemSdfGradient")
+        return float(loss), g
+
+    def train(self, samples: torch.Tensor, shapes: torch.Tensor | None = None,
+              epochs: int = 10, batch: int = 8192, lr: float = 2e-3, band: float = 0.0) -> float:
+        loss = lib.fcdemSdfTrainSamples(self._h, _p(samples), _opt(shapes), samples.shape[0],
+                                        epochs, batch, lr, band)
+        check("fcdemSdfTrainSamples")
+        return float(loss)
+
+    def eval_f32(self, pts: torch.Tensor, shapes: torch.Tensor | None = None) -> torch.Tensor:
+        d = torch.empty(pts.shape[0], dtype=torch.float32, device=pts.device)
+        lib.fcdemSdfEvalF32(self._h, _p(pts), _opt(shapes), pts.shape[0], _p(d))
+        check("fcdemSdfEvalF32")
+        return d
+
+    def infer(self, pts: torch.Tensor, shapes: torch.Tensor | None = None) -> torch.Tensor:
+        d = torch.empty(pts.shape[0], dtype=torch.float32, device=pts.device)
+        lib.fcdemSdfInfer(self._h, _p(pts), _opt(shapes), pts.shape[0], _p(d))
+        check("fcdemSdfInfer")
+        return d
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib.fcdemSdfDestroy(h)
+            self._h = None
+
+
+def samples(dmap: DistanceMap, n: int, near_fraction: float = 0.5, band: float = 0.05,
+            seed: int = 7, shape: int | None = None, device="cuda"):
+    """n training samples (x, y, z, distance) of the map; with `shape`, also
+    the int32 shape codes."""
+    s = torch.empty((n, 4), dtype=torch.float32, device=device)
+    sh = torch.empty(n, dtype=torch.int32, device=device) if shape is not None else None
+    lib.fcdemSdfSamples(dmap.handle, -1 if shape is None else shape, n, near_fraction, band,
+                        seed, _p(s), _opt(sh))
+    check("fcdemSdfSamples")
+    return (s, sh) if shape is not None else s
+
+
+def um_integrate_system_sdf(pos, vel, dt: float, n: int, dmap: DistanceMap, net: SdfNet,
+                            skin: float, exact_counter: torch.Tensor | None = None) -> None:
+    lib.fcdemUM_integrateSystemSdf(_p(pos), _p(vel), dt, n, dmap.handle, net.handle, skin,
+                                   _opt(exact_counter))

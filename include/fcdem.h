@@ -290,6 +290,71 @@ void fcdemUM_reorderDataAndFindCellStart(uint *cellStart, uint *cellEnd, float *
                                          uint numParticles, uint numCells);
 
 /* ---------------------------------------------------------------------- */
+/* Neural signed-distance field of an obstacle (no counterpart in the
+ * reference).  A small MLP -- inputs (x, y, z) normalised as
+ * (x - shift) * scale, optionally a one-hot shape code, `hiddenLayers` SiLU
+ * layers of width `hidden` (64 or 128), one linear output times outScale --
+ * predicts the distance the map query returns.  Trained on the GPU (FP32
+ * forward/backward kernels, Adam) on samples of a distance map; inference
+ * runs with BF16 weights and activations on the tensor cores (FP32
+ * accumulate).  In the culled boundary integrate the exact map query stays
+ * the fallback inside the skin band. */
+typedef struct fcdemSdfNet fcdemSdfNet;
+
+/* inputs: 3 + number of shape codes (at most 16); hidden: 64 or 128;
+ * hiddenLayers: 2 or 3.  Weights uniform in +-sqrt(6 / fan_in), biases 0. */
+fcdemSdfNet *fcdemSdfCreate(int inputs, int hidden, int hiddenLayers,
+                            unsigned long long seed);
+void fcdemSdfDestroy(fcdemSdfNet *net);
+uint fcdemSdfNumParams(const fcdemSdfNet *net);
+/* FP32 parameter vector (host): W0 [hidden][inputs], b0, per further hidden
+ * layer W [hidden][hidden], b, then wOut [hidden], bOut; row-major [out][in]. */
+void fcdemSdfGetParams(const fcdemSdfNet *net, float *host);
+void fcdemSdfSetParams(fcdemSdfNet *net, const float *host);
+void fcdemSdfSetNormalization(fcdemSdfNet *net, const float shift[3], const float scale[3],
+                              float outScale);
+void fcdemSdfGetNormalization(const fcdemSdfNet *net, float shift[3], float scale[3],
+                              float *outScale);
+/* n training samples (device float4: x, y, z, map distance) in the map box:
+ * the first nearFraction * n drawn until |distance| < band, the others
+ * uniform.  shapes (device int[n], optional) receives `shape`. */
+void fcdemSdfSamples(const fcdemDistanceMap *map, int shape, uint n, float nearFraction,
+                     float band, unsigned long long seed, float *samples4, int *shapes);
+/* Loss sum_s w_s (y_s - d_s / outScale)^2 / n, w_s = 10 when |d_s| < band
+ * else 1, and its gradient (host float[numParams], optional) for the device
+ * samples. */
+float fcdemSdfGradient(fcdemSdfNet *net, const float *samples4, const int *shapes, uint n,
+                       float band, float *gradHost);
+/* Adam over `epochs` passes of mini-batches of `batch` samples, learning rate
+ * lr with cosine decay to lr / 20.  Returns the last epoch's mean loss. */
+float fcdemSdfTrainSamples(fcdemSdfNet *net, const float *samples4, const int *shapes, uint n,
+                           uint epochs, uint batch, float lr, float band);
+/* Distance predictions d[n] at device points (float4, w ignored): FP32 on
+ * the CUDA cores, or BF16 on the tensor cores. */
+void fcdemSdfEvalF32(fcdemSdfNet *net, const float *points4, const int *shapes, uint n,
+                     float *d);
+void fcdemSdfInfer(fcdemSdfNet *net, const float *points4, const int *shapes, uint n,
+                   float *d);
+/* `steps` unified-memory DEM steps (CollisionPipeline<dem_gpu_unified>::
+ * startPipeline, dempipeline.hpp:113-120: calcHash, sortParticles,
+ * reorderDataAndFindCellStart, evalForces, integrateSystem with the map
+ * boundary) in one call.  force (float3[n], optional) receives evalForces'
+ * force of the last step.  With net, the integrate culls the map query as
+ * fcdemUM_integrateSystemSdf.  On return every array holds what the staged
+ * calls leave (cellEnd of empty cells aside). */
+void fcdemUM_update(float *pos, float *vel, float *force, float *sortedPos, float *sortedVel,
+                    uint *hash, uint *index, uint *cellStart, uint *cellEnd, float deltaTime,
+                    uint numParticles, uint numCells, uint steps, const fcdemDistanceMap *map,
+                    fcdemSdfNet *net, float skin, uint *exactQueries);
+
+/* fcdemUM_integrateSystem with the map query made only where the particle is
+ * in the map box and the network predicts a distance of at most `skin`;
+ * exactQueries (device counter, optional) is incremented per exact query. */
+void fcdemUM_integrateSystemSdf(float *pos, float *vel, float deltaTime, uint numParticles,
+                                const fcdemDistanceMap *map, fcdemSdfNet *net, float skin,
+                                uint *exactQueries);
+
+/* ---------------------------------------------------------------------- */
 /* Batches: many independent scenes stepped together (no counterpart in the
  * reference, which steps one ParticleSystem at a time).  Every scene has its
  * own SimParams (grid, cell size, origin, contact parameters), its own box

@@ -1,0 +1,198 @@
+"""Neural SDF: the training kernels' gradients against the FP64 oracle, the
+FP32 forward and the BF16 tensor-core inference against plain PyTorch
+references, and the culled boundary integrate: what the trained network
+saves (exact map queries) with results identical to the method without it."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import sdf_oracle as so
+
+pytestmark = pytest.mark.gpu
+
+CONFIGS = [(3, 64, 3), (11, 128, 2), (3, 64, 2), (3, 128, 3)]
+
+
+def _torus():
+    from fullc0ntact_gb300 import dem
+    return dem.DistanceMap.torus(0.3, 0.1, 128, 0.05)
+
+
+def _net(inputs, hidden, layers, dmap, seed=11, jitter=0.0):
+    from fullc0ntact_gb300.sdf import SdfNet
+    net = SdfNet(inputs, hidden, layers, seed=seed)
+    net.normalize_to(dmap)
+    if jitter:
+        p = net.get_params()
+        rng = np.random.default_rng(seed)
+        net.set_params(p + rng.normal(0.0, jitter, p.shape).astype(np.float32))
+    return net
+
+
+def _torch_forward(net, pts, shapes=None, bf16=False):
+    """Plain PyTorch fp32 forward of the network (with bf16=True: the hidden
+    layers' operands rounded to bf16, fp32 accumulation -- the tensor-core
+    kernel's arithmetic)."""
+    lay = so.layout(net.inputs, net.hidden, net.layers)
+    p = torch.from_numpy(net.get_params()).to(pts.device)
+    shift, scale, out_scale = net.normalization()
+    H = net.hidden
+    X = torch.zeros((pts.shape[0], net.inputs), device=pts.device)
+    X[:, :3] = (pts[:, :3] - torch.from_numpy(shift).to(pts.device)) * \
+        torch.from_numpy(scale).to(pts.device)
+    if shapes is not None and net.inputs > 3:
+        X[torch.arange(pts.shape[0], device=pts.device), 3 + shapes.long()] = 1.0
+    h = X
+    for l, ((o, (r, c)), bo) in enumerate(zip(lay["W"], lay["b"])):
+        W = p[o:o + r * c].view(r, c)
+        b = p[bo:bo + H]
+        if bf16 and l >= 1:
+            z = h.to(torch.bfloat16).float() @ W.to(torch.bfloat16).float().T + b
+        else:
+            z = h @ W.T + b
+        h = torch.nn.functional.silu(z)
+    y = h @ p[lay["wo"]:lay["wo"] + H] + p[lay["bo"]]
+    return y * out_scale
+
+
+@pytest.mark.parametrize("cfg", CONFIGS)
+def test_layout_matches_oracle(cfg):
+    dmap = _torus()
+    net = _net(*cfg, dmap)
+    assert net.num_params == so.layout(*cfg)["total"]
+    p = net.get_params()
+    net.set_params(p * 0.5)
+    np.testing.assert_array_equal(net.get_params(), p * 0.5)
+
+
+@pytest.mark.parametrize("cfg", CONFIGS)
+def test_training_gradient_matches_fp64_oracle(cfg):
+    """fcdemSdfGradient (FP32 forward/backward kernels, atomics over tiles)
+    against the FP64 oracle on the same parameters and samples; a batch that
+    is not a multiple of the tile, samples on both sides of the band."""
+    from fullc0ntact_gb300 import sdf
+    dmap = _torus()
+    net = _net(*cfg, dmap, jitter=0.05)
+    n = 1000
+    shapes = None
+    if cfg[0] > 3:
+        s, shapes = sdf.samples(dmap, n, 0.5, 0.05, seed=3, shape=0)
+        shapes = torch.randint(0, cfg[0] - 3, (n,), device="cuda", dtype=torch.int32)
+    else:
+        s = sdf.samples(dmap, n, 0.5, 0.05, seed=3)
+    band = 0.02
+    loss, g = net.gradient(s, shapes, band)
+    shift, scale, out_scale = net.normalization()
+    lay = so.layout(*cfg)
+    lref, gref = so.loss_and_grad(net.get_params().astype(np.float64), lay,
+                                  s.cpu().numpy().astype(np.float64),
+                                  None if shapes is None else shapes.cpu().numpy(),
+                                  band, shift, scale, out_scale)
+    assert abs(loss - lref) <= 1e-5 * abs(lref) + 1e-7
+    err = np.abs(g.astype(np.float64) - gref)
+    # FP32 sums over 1000 samples: 1e-4 of the gradient's scale per element
+    scale_g = np.max(np.abs(gref))
+    assert np.max(err) <= 1e-4 * scale_g, (np.max(err), scale_g)
+    assert np.linalg.norm(err) <= 1e-5 * np.linalg.norm(gref) * 10
+
+
+@pytest.mark.parametrize("cfg", CONFIGS)
+def test_fp32_forward_matches_torch(cfg):
+    from fullc0ntact_gb300 import sdf
+    dmap = _torus()
+    net = _net(*cfg, dmap, jitter=0.05)
+    s = sdf.samples(dmap, 5000, 0.3, 0.05, seed=4)
+    shapes = (torch.randint(0, cfg[0] - 3, (5000,), device="cuda", dtype=torch.int32)
+              if cfg[0] > 3 else None)
+    d = net.eval_f32(s, shapes)
+    ref = _torch_forward(net, s, shapes)
+    tol = 1e-5 * float(ref.abs().max()) + 1e-6
+    assert float((d - ref).abs().max()) <= tol
+
+
+@pytest.mark.parametrize("cfg", CONFIGS)
+def test_tensor_core_inference_matches_bf16_reference(cfg):
+    """kSdfInfer (tcgen05.mma, BF16 operands, FP32 accumulation in TMEM)
+    against the PyTorch fp32 forward with the same operands rounded to bf16;
+    ragged tail (n not a multiple of the 128-point tile)."""
+    from fullc0ntact_gb300 import sdf
+    dmap = _torus()
+    net = _net(*cfg, dmap, jitter=0.05)
+    n = 100_003
+    s = sdf.samples(dmap, n, 0.3, 0.05, seed=5)
+    shapes = (torch.randint(0, cfg[0] - 3, (n,), device="cuda", dtype=torch.int32)
+              if cfg[0] > 3 else None)
+    d = net.infer(s, shapes)
+    ref = _torch_forward(net, s, shapes, bf16=True)
+    diff = (d - ref).abs()
+    scale = float(ref.abs().max())
+    q999 = float(torch.quantile(diff[:100_000], 0.999))
+    print(f"cfg {cfg}: max {float(diff.max()):.3e} mean {float(diff.mean()):.3e} "
+          f"q99.9 {q999:.3e} scale {scale:.3e}")
+    # The FP32 sums run in another order than PyTorch's, so an activation
+    # near a bf16 rounding boundary can round the other way (one bf16 ulp,
+    # 2^-8 relative) and move that prediction; most predictions agree to
+    # FP32 accumulation noise.
+    assert float(diff.max()) <= 5e-3 * scale, (float(diff.max()), scale)
+    assert q999 <= 5e-4 * scale, (q999, scale)
+    assert float(diff.mean()) <= 2e-5 * scale
+    # and close to the fp32 network
+    f32 = _torch_forward(net, s, shapes)
+    assert float((d - f32).abs().max()) <= 3e-2 * scale
+
+
+def test_trained_network_culls_exact_queries_without_changing_results():
+    """Config-2 network (3 -> 64 -> 64 -> 64 -> 1) trained on 2M samples of
+    the 128^3 torus map.  Judged by the exact map: no point the map puts
+    within one particle radius is predicted above the skin band (2 radii),
+    and near the surface the error stays below one radius.  The culled
+    boundary integrate then gives bit-identical positions and velocities
+    while making a small fraction of the exact map queries that the method
+    without the network makes (one per particle in the map box)."""
+    from fullc0ntact_gb300 import dem, sdf
+    from fullc0ntact_gb300.params import make_params
+    dmap = _torus()
+    net = _net(3, 64, 3, dmap, seed=5)
+    r = 1.0 / 256.0
+    skin = 2.0 * r
+    train = sdf.samples(dmap, 2_000_000, 0.6, 0.05, seed=21)
+    loss = net.train(train, epochs=20, batch=2048, lr=5e-3, band=0.02)
+    assert loss < 1e-4
+    val = sdf.samples(dmap, 400_000, 0.5, 0.03, seed=99)
+    pred = net.infer(val)
+    d = val[:, 3]
+    touching = d < r
+    assert int(touching.sum()) > 1000
+    assert int((touching & (pred > skin)).sum()) == 0
+    near = d.abs() < 0.02
+    assert float((pred - d)[near].abs().max()) < r
+    # particles around the torus (none inside it), in and out of the map box
+    n = 300_000
+    g = torch.Generator(device="cuda").manual_seed(8)
+    pos = torch.zeros((3 * n, 4), device="cuda")
+    pos[:, :3] = (torch.rand((3 * n, 3), device="cuda", generator=g) * 2 - 1) * \
+        torch.tensor([0.55, 0.55, 0.25], device="cuda")
+    dist, _ = dmap.query(pos)
+    pos = pos[dist > r][:n].contiguous()
+    assert pos.shape[0] == n
+    pos[:, 3] = 1.0
+    vel = torch.zeros((n, 4), device="cuda")
+    vel[:, :3] = (torch.rand((n, 3), device="cuda", generator=g) * 2 - 1) * 0.002
+    dem.set_parameters(make_params(n, (128, 128, 128), r, gravity=(0.0, 0.0, -3e-4)))
+    pa, va = pos.clone(), vel.clone()
+    pb, vb = pos.clone(), vel.clone()
+    counter = torch.zeros(1, dtype=torch.int32, device="cuda")
+    steps = 3
+    for _ in range(steps):
+        dem.um_integrate_system(pa, va, 0.5, n, dmap)
+        sdf.um_integrate_system_sdf(pb, vb, 0.5, n, dmap, net, skin, counter)
+    dem.check("integrate")
+    np.testing.assert_array_equal(pa.cpu().numpy().view(np.uint32),
+                                  pb.cpu().numpy().view(np.uint32))
+    np.testing.assert_array_equal(va.cpu().numpy().view(np.uint32),
+                                  vb.cpu().numpy().view(np.uint32))
+    lo, hi = torch.from_numpy(dmap.vmin).cuda(), torch.from_numpy(dmap.vmax).cuda()
+    in_box = int(((pos[:, :3] >= lo) & (pos[:, :3] <= hi)).all(1).sum()) * steps
+    exact = int(counter.item())
+    print(f"exact map queries: {exact} of {in_box} in-box particle steps")
+    assert exact < 0.15 * in_box, (exact, in_box)
