@@ -61,6 +61,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the batched-scenes measurement")
+    ap.add_argument("--no-config2", action="store_true",
+                    help="skip the torus-obstacle (distance map / neural SDF) measurement")
+    ap.add_argument("--config2-n", type=int, default=1048576)
+    ap.add_argument("--config2-steps", type=int, default=200)
     ap.add_argument("--batch-scenes", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=20)
     return ap.parse_args()
@@ -239,6 +243,118 @@ def measure_batched(num_scenes: int, steps: int, dev: int) -> dict:
             "plain_per_scene": {"value": pv, "ms_per_step": plain_ms / steps},
             "speedup": bv / pv, "unit": UNIT,
             "equal_results": "bit-identical per scene (tests/test_gpu_batch.py)"}
+
+
+def measured_peak_tflops():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured"
+    except Exception:
+        return 1900.0, "fallback"
+
+
+def measure_config2(n: int, steps: int, dev: int) -> dict:
+    """Spheres falling onto the torus obstacle (128^3 distance map) through
+    the fused unified-memory step: plain (exact map query for every particle
+    in the map box) and with the neural SDF culling the query (3 -> 64 -> 64
+    -> 64 -> 1 SiLU network trained on 2M map samples; skin 2 radii).  Both
+    from the same initial state; CUDA events on the stream."""
+    import ctypes as C
+    import torch
+    from fullc0ntact_gb300 import dem, scenes, sdf
+    lib = dem.lib
+    dmap = dem.DistanceMap.torus(0.3, 0.1, 128, 0.05)
+    net = sdf.SdfNet(3, 64, 3, seed=5)
+    net.normalize_to(dmap)
+    train = sdf.samples(dmap, 2_000_000, 0.6, 0.05, seed=21)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    loss = net.train(train, epochs=20, batch=2048, lr=5e-3, band=0.02)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    del train
+    # judge: the exact map on held-out samples
+    val = sdf.samples(dmap, 1_048_576, 0.5, 0.03, seed=99)
+    sc = scenes.config2(n)
+    r = sc["radius"]
+    skin = 2.0 * r
+    pred = net.infer(val)
+    d = val[:, 3]
+    near = d.abs() < 0.02
+    judge = {"samples": int(val.shape[0]),
+             "max_abs_err_within_0.02": float((pred - d)[near].abs().max()),
+             "rms_err_within_0.02": float((pred - d)[near].pow(2).mean().sqrt()),
+             "touching_points_predicted_above_skin":
+                 int(((d < r) & (pred > skin)).sum())}
+    # tensor-core inference alone on the held-out points
+    for _ in range(3):
+        net.infer(val)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    reps = 20
+    for _ in range(reps):
+        net.infer(val)
+    e1.record()
+    torch.cuda.synchronize()
+    infer_ms = e0.elapsed_time(e1) / reps
+    tc_flop = 2.0 * 2 * 64 * 64 * val.shape[0]  # the two 64x64 layers on the tensor cores
+    peak_tf, peak_kind = measured_peak_tflops()
+    lib.fcdemSetProfiling.argtypes = [C.c_int]
+    lib.fcdemGetStageTimes.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_uint), C.c_int]
+    out = {}
+    finals = {}
+    for mode in ("plain", "neural"):
+        us = dem.UmScene(sc, dmap, f"cuda:{dev}")
+        counter = torch.zeros(1, dtype=torch.int32, device=us.pos.device)
+        kw = dict(net=net, skin=skin, exact_counter=counter) if mode == "neural" else {}
+        us.update(3, **kw)  # warm-up
+        us.pos.copy_(torch.from_numpy(sc["pos"]))
+        us.vel.copy_(torch.from_numpy(sc["vel"]))
+        counter.zero_()
+        torch.cuda.synchronize()
+        e0.record()
+        us.update(steps, force=False, **kw)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        dem.check(f"config2 {mode}")
+        finals[mode] = (us.pos.clone(), us.vel.clone())
+        exact = int(counter.item())
+        # stage attribution over the same steps
+        us.pos.copy_(torch.from_numpy(sc["pos"]))
+        us.vel.copy_(torch.from_numpy(sc["vel"]))
+        lib.fcdemSetProfiling(1)
+        us.update(steps, force=False, **kw)
+        st = (C.c_float * 5)()
+        cnt = (C.c_uint * 5)()
+        lib.fcdemGetStageTimes(st, cnt, 5)
+        lib.fcdemSetProfiling(0)
+        dem.check(f"config2 {mode} stages")
+        names = ["integrate_hash", "sort", "tables", "reorder", "collide"]
+        out[mode] = {"value": n * steps / (ms / 1e3), "ms_per_step": ms / steps,
+                     "stage_ms_per_step": {names[k]: (st[k] / steps if cnt[k] else None)
+                                           for k in range(5)}}
+        if mode == "neural":
+            out[mode]["exact_map_queries_per_step"] = exact / steps
+        del us
+    same = all(torch.equal(a.view(torch.int32), b.view(torch.int32))
+               for a, b in zip(finals["plain"], finals["neural"]))
+    return {"workload": f"{n} spheres r=1/256 falling onto a torus (R 0.3, r 0.1), 128^3 "
+                        "distance map, unified-memory step (calcHash, sort, reorder, "
+                        f"evalForces, integrate with map/cylinder/planes), {steps} steps",
+            "n": n, "steps": steps, "unit": UNIT,
+            "plain_exact_map": out["plain"], "neural_sdf": out["neural"],
+            "speedup": out["neural"]["value"] / out["plain"]["value"],
+            "equal_final_state": bool(same),
+            "network": {"layers": "3-64-64-64-1 SiLU", "params": net.num_params,
+                        "train_samples": 2_000_000, "epochs": 20, "train_s": train_s,
+                        "final_loss": loss, "judge": judge},
+            "tensor_core_inference": {"points": int(val.shape[0]), "ms": infer_ms,
+                                      "tc_tflops": tc_flop / (infer_ms / 1e3) / 1e12,
+                                      "peak_tflops": peak_tf, "peak_source": peak_kind,
+                                      "frac": tc_flop / (infer_ms / 1e3) / 1e12 / peak_tf}}
 
 
 def cpu_baseline(sc: dict, steps: int) -> dict:
@@ -444,6 +560,11 @@ def run_ours(args):
     e2e = replica_throughput(n, e2e_steps, e2e_s, world)
     clk = clocks.stop()
 
+    config2 = None
+    if not args.no_config2:
+        config2 = measure_config2(args.config2_n, args.config2_steps, dev)
+        torch.cuda.empty_cache()
+
     batched = None
     if not args.no_batched:
         del ds  # free the large scene's arrays first
@@ -479,6 +600,7 @@ def run_ours(args):
             "phases": phases,
             "final_cells": final_cells,
             "batched": batched,
+            "config2": config2,
             "clocks": clk,
             "cpu_baseline": cpu,
         }

@@ -91,15 +91,27 @@ __device__ __forceinline__ float queryMap(const MapView &M, float3 q, float3 &cp
   const float d1 = (float)((double)d01 * wy + (double)__fmul_rn(d11, yd));
   const float dist = (float)((double)d0 * wz + (double)__fmul_rn(d1, zd));
   // trilinearInterpolateCP (distancemap.cuh:254-279): Vector3<float> times the
-  // weight converted to float
+  // weight converted to float.  Every sum a * w0 + b * w1 is written as
+  // fmaf(a, w0, b * w1) with the second product rounded (lerp): each kernel
+  // that inlines this function gets the same bits.
   const float fwx = (float)wx, fwy = (float)wy, fwz = (float)wz;
-  float3 a00 = make_float3(c0.y * fwx + c1.y * xd, c0.z * fwx + c1.z * xd, c0.w * fwx + c1.w * xd);
-  float3 a10 = make_float3(c3.y * fwx + c2.y * xd, c3.z * fwx + c2.z * xd, c3.w * fwx + c2.w * xd);
-  float3 a01 = make_float3(c4.y * fwx + c5.y * xd, c4.z * fwx + c5.z * xd, c4.w * fwx + c5.w * xd);
-  float3 a11 = make_float3(c7.y * fwx + c6.y * xd, c7.z * fwx + c6.z * xd, c7.w * fwx + c6.w * xd);
-  float3 a0 = make_float3(a00.x * fwy + a10.x * yd, a00.y * fwy + a10.y * yd, a00.z * fwy + a10.z * yd);
-  float3 a1 = make_float3(a01.x * fwy + a11.x * yd, a01.y * fwy + a11.y * yd, a01.z * fwy + a11.z * yd);
-  cp = make_float3(a0.x * fwz + a1.x * zd, a0.y * fwz + a1.y * zd, a0.z * fwz + a1.z * zd);
+  auto lerp = [](float a, float w0, float b, float w1) {
+    return fmaf(a, w0, __fmul_rn(b, w1));
+  };
+  float3 a00 = make_float3(lerp(c0.y, fwx, c1.y, xd), lerp(c0.z, fwx, c1.z, xd),
+                           lerp(c0.w, fwx, c1.w, xd));
+  float3 a10 = make_float3(lerp(c3.y, fwx, c2.y, xd), lerp(c3.z, fwx, c2.z, xd),
+                           lerp(c3.w, fwx, c2.w, xd));
+  float3 a01 = make_float3(lerp(c4.y, fwx, c5.y, xd), lerp(c4.z, fwx, c5.z, xd),
+                           lerp(c4.w, fwx, c5.w, xd));
+  float3 a11 = make_float3(lerp(c7.y, fwx, c6.y, xd), lerp(c7.z, fwx, c6.z, xd),
+                           lerp(c7.w, fwx, c6.w, xd));
+  float3 a0 = make_float3(lerp(a00.x, fwy, a10.x, yd), lerp(a00.y, fwy, a10.y, yd),
+                          lerp(a00.z, fwy, a10.z, yd));
+  float3 a1 = make_float3(lerp(a01.x, fwy, a11.x, yd), lerp(a01.y, fwy, a11.y, yd),
+                          lerp(a01.z, fwy, a11.z, yd));
+  cp = make_float3(lerp(a0.x, fwz, a1.x, zd), lerp(a0.y, fwz, a1.y, zd),
+                   lerp(a0.z, fwz, a1.z, zd));
   return dist;
 }
 
@@ -109,52 +121,57 @@ __device__ __forceinline__ void checkDistMap(const MapView &M, float radius, flo
   float3 cp = make_float3(0.0f, 0.0f, 0.0f);
   const float dist = queryMap(M, pos, cp);
   if (dist < radius) {
+    // the roundings are spelled out (fmaf, __fmul_rn) so that every kernel
+    // inlining this function computes the same bits
     float3 n0 = make_float3(pos.x - cp.x, pos.y - cp.y, pos.z - cp.z);
-    float invLen = rsqrtf(n0.x * n0.x + n0.y * n0.y + n0.z * n0.z);
-    float3 n = make_float3(n0.x * invLen, n0.y * invLen, n0.z * invLen);
+    float invLen = rsqrtf(fmaf(n0.x, n0.x, fmaf(n0.y, n0.y, __fmul_rn(n0.z, n0.z))));
+    float3 n = make_float3(__fmul_rn(n0.x, invLen), __fmul_rn(n0.y, invLen),
+                           __fmul_rn(n0.z, invLen));
     float pen = radius - dist;
     float extra = (float)(0.1 * (double)radius);
-    pos = make_float3(pos.x + n.x * pen, pos.y + n.y * pen, pos.z + n.z * pen);
-    pos = make_float3(pos.x + n.x * extra, pos.y + n.y * extra, pos.z + n.z * extra);
-    vel.x = vel.x * (0.5f * bd);
-    vel.y = vel.y * (0.5f * bd);
-    vel.z = vel.z * (0.7f * bd);
+    pos = make_float3(fmaf(n.x, pen, pos.x), fmaf(n.y, pen, pos.y), fmaf(n.z, pen, pos.z));
+    pos = make_float3(fmaf(n.x, extra, pos.x), fmaf(n.y, extra, pos.y), fmaf(n.z, extra, pos.z));
+    vel.x = __fmul_rn(vel.x, 0.5f * bd);
+    vel.y = __fmul_rn(vel.y, 0.5f * bd);
+    vel.z = __fmul_rn(vel.z, 0.7f * bd);
   }
 }
 
 // The velocity and position update of d_integrateSystem
 // (particledem_um.cu:604-638).
 __device__ __forceinline__ void umAdvance(float3 &p, float3 &v, float dt, const SimParams &P) {
-  v.x = v.x + P.gravity[0] * dt;
-  v.y = v.y + P.gravity[1] * dt;
-  v.z = v.z + P.gravity[2] * dt;
-  v.x = v.x * P.globalDamping;
-  v.y = v.y * P.globalDamping;
-  v.z = v.z * P.globalDamping;
-  p.x = p.x + v.x * dt;
-  p.y = p.y + v.y * dt;
-  p.z = p.z + v.z * dt;
+  v.x = fmaf(P.gravity[0], dt, v.x);
+  v.y = fmaf(P.gravity[1], dt, v.y);
+  v.z = fmaf(P.gravity[2], dt, v.z);
+  v.x = __fmul_rn(v.x, P.globalDamping);
+  v.y = __fmul_rn(v.y, P.globalDamping);
+  v.z = __fmul_rn(v.z, P.globalDamping);
+  p.x = fmaf(v.x, dt, p.x);
+  p.y = fmaf(v.y, dt, p.y);
+  p.z = fmaf(v.z, dt, p.z);
 }
 
 // The rest of it: the map contact (when `mapTest`), the r = 1 cylinder
 // around z, tested with the position before the map push, and the z planes
-// at -1 and 10 (d_checkBoundaryDistMap, boundaries.cuh:65-89).
+// at -1 and 10 (d_checkBoundaryDistMap, boundaries.cuh:65-89).  Roundings
+// spelled out as in checkDistMap.
 __device__ __forceinline__ void umBoundary(const MapView &M, bool mapTest, float r, float bd,
                                            float3 &p, float3 &v) {
   const float px0 = p.x, py0 = p.y;
-  const float len = sqrtf(px0 * px0 + py0 * py0 + 0.0f * 0.0f);
+  const float l2 = fmaf(px0, px0, __fmul_rn(py0, py0));  // + 0.0f * 0.0f: exact
+  const float len = sqrtf(l2);
   if (mapTest) checkDistMap(M, r, bd, p, v);
   if (len > 1.0f) {
-    float pen = len - 1.0f;
-    float invLen = rsqrtf(px0 * px0 + py0 * py0 + 0.0f * 0.0f);
-    float3 nn = make_float3(px0 * invLen, py0 * invLen, 0.0f * invLen);
-    float s = pen + r;
-    p = make_float3(p.x - nn.x * s, p.y - nn.y * s, p.z - nn.z * s);
-    v.x = v.x * bd;
-    v.y = v.y * bd;
+    const float pen = len - 1.0f;
+    const float invLen = rsqrtf(l2);
+    const float3 nn = make_float3(__fmul_rn(px0, invLen), __fmul_rn(py0, invLen), 0.0f);
+    const float s = pen + r;
+    p = make_float3(fmaf(-nn.x, s, p.x), fmaf(-nn.y, s, p.y), fmaf(-nn.z, s, p.z));
+    v.x = __fmul_rn(v.x, bd);
+    v.y = __fmul_rn(v.y, bd);
   }
-  if (p.z > 10.0f - r) { p.z = 10.0f - r; v.z = v.z * bd; }
-  if (p.z < -1.0f + r) { p.z = -1.0f + r; v.z = v.z * bd; }
+  if (p.z > 10.0f - r) { p.z = 10.0f - r; v.z = __fmul_rn(v.z, bd); }
+  if (p.z < -1.0f + r) { p.z = -1.0f + r; v.z = __fmul_rn(v.z, bd); }
 }
 
 // Inside the map box (where queryMap reads the map rather than 5.0).

@@ -79,6 +79,11 @@ struct SdfView {
 
 __device__ __forceinline__ float sigm(float z) { return 1.0f / (1.0f + expf(-z)); }
 __device__ __forceinline__ float silu(float z) { return z * sigm(z); }
+// Inference SiLU: fast exponential and division (a few ulp of FP32, far
+// below the bf16 rounding of the activations it feeds).
+__device__ __forceinline__ float siluFast(float z) {
+  return z * __fdividef(1.0f, 1.0f + __expf(-z));
+}
 __device__ __forceinline__ float dsilu(float z) {
   const float s = sigm(z);
   return s * (1.0f + z * (1.0f - s));
@@ -522,7 +527,7 @@ __device__ __forceinline__ bool sdfTileForward(SdfTileSmem<H, L> &sm, const SdfV
       z = fmaf(w[1], x1, z);
       z = fmaf(w[2], x2, z);
       if (shape >= 0 && 3 + shape < D) z += w[3 + shape];
-      h[u] = silu(z);
+      h[u] = siluFast(z);
     }
     uint4 v = make_uint4(packBf16(h[0], h[1]), packBf16(h[2], h[3]), packBf16(h[4], h[5]),
                          packBf16(h[6], h[7]));
@@ -562,7 +567,7 @@ __device__ __forceinline__ bool sdfTileForward(SdfTileSmem<H, L> &sm, const SdfV
       tmemLoad16(sm.tmem + ((unsigned)(32 * warp) << 16) + (unsigned)(c * 16), r);
       tmemWaitLoad();
 #pragma unroll
-      for (int u = 0; u < 16; ++u) r[u] = silu(r[u] + sm.b[l * H + c * 16 + u]);
+      for (int u = 0; u < 16; ++u) r[u] = siluFast(r[u] + sm.b[l * H + c * 16 + u]);
       if (last) {
 #pragma unroll
         for (int u = 0; u < 16; ++u) y = fmaf(r[u], sm.wo[c * 16 + u], y);
@@ -640,9 +645,12 @@ kIntegrateSdf(float4 *__restrict__ pos, float4 *__restrict__ vel, float dt, unsi
     float3 p = make_float3(p4.x, p4.y, p4.z), v = make_float3(v4.x, v4.y, v4.z);
     const float r = kp.radiusFromW ? p4.w : P.particleRadius;
     umAdvance(p, v, dt, P);
-    const bool inBox = inMapBox(M, p);
+    const bool inBox = valid && inMapBox(M, p);
     float dPred = 0.0f;
-    if (!sdfTileForward<H, L>(sm, net, (p.x - net.shift[0]) * net.scale[0],
+    // a tile with no particle in the map box needs no prediction (the map
+    // reads 5.0 outside its box); the decision is the same for every thread
+    if (__syncthreads_or(inBox) &&
+        !sdfTileForward<H, L>(sm, net, (p.x - net.shift[0]) * net.scale[0],
                               (p.y - net.shift[1]) * net.scale[1],
                               (p.z - net.shift[2]) * net.scale[2], 0, phase, dPred)) {
       if (threadIdx.x == 0) atomicOr(status, (unsigned)kStatusTimeout);
@@ -805,7 +813,14 @@ bool adamStep(fcdemSdfNet *net, float lr) {
   return launchOk();
 }
 
-constexpr unsigned kSdfCtasPerSm = 3;
+// CTAs per SM that fit both the shared memory (227 KB) and the 512 TMEM
+// columns (H per CTA); the persistent grid is 152 times that.
+template <int H, int L>
+constexpr unsigned sdfCtasPerSm() {
+  constexpr unsigned bySmem = (unsigned)((227u * 1024u) / (sizeof(SdfTileSmem<H, L>) + 1024u));
+  constexpr unsigned byTmem = 512u / (unsigned)H;
+  return bySmem < byTmem ? bySmem : byTmem;
+}
 
 template <int H, int L>
 bool launchInfer(fcdemSdfNet *net, const float4 *pts, const int *shapes, unsigned n,
@@ -813,7 +828,7 @@ bool launchInfer(fcdemSdfNet *net, const float4 *pts, const int *shapes, unsigne
   const size_t smem = tileSmemBytes<H, L>();
   cudaFuncSetAttribute(kSdfInfer<H, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   unsigned grid = (n + 127) / 128;
-  if (grid > 152u * kSdfCtasPerSm) grid = 152u * kSdfCtasPerSm;
+  if (grid > 152u * sdfCtasPerSm<H, L>()) grid = 152u * sdfCtasPerSm<H, L>();
   kSdfInfer<H, L><<<grid, 128, smem, curStream()>>>(sdfView(net), pts, shapes, n, d,
                                                     ctx().dStatus);
   return launchOk();
@@ -825,7 +840,7 @@ bool launchIntegrateSdf(fcdemSdfNet *net, float4 *pos, float4 *vel, float dt, un
                         const UmCount *count) {
   const size_t smem = tileSmemBytes<H, L>();
   unsigned grid = (n + 127) / 128;
-  if (grid > 152u * kSdfCtasPerSm) grid = 152u * kSdfCtasPerSm;
+  if (grid > 152u * sdfCtasPerSm<H, L>()) grid = 152u * sdfCtasPerSm<H, L>();
   if (count) {
     cudaFuncSetAttribute(kIntegrateSdf<H, L, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
