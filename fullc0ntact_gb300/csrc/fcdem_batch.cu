@@ -11,7 +11,7 @@
 #include <cstring>
 #include <vector>
 
-#include "fcdem_internal.cuh"
+#include "fcdem_map.cuh"
 
 struct fcdemBatch {
   int device = -1;
@@ -31,6 +31,12 @@ struct fcdemBatch {
   const void *gPos = nullptr, *gVel = nullptr;
   float gDt = 0.0f;
   unsigned gSteps = 0;
+  // obstacles (fcdemBatchSetObstacles)
+  std::vector<fcdem::BatchScene> hostScenes;
+  fcdem::MapView *maps = nullptr;  // device, one per shape
+  fcdemSdfNet *net = nullptr;
+  float skin = 0.0f;
+  unsigned *exact = nullptr;  // device counter of exact map queries
 };
 
 namespace fcdem {
@@ -49,15 +55,47 @@ void freeBatch(fcdemBatch *b) {
   cudaFree(b->hash);
   cudaFree(b->index);
   cudaFree(b->countBuf);
+  cudaFree(b->maps);
+  cudaFree(b->exact);
   delete b;
 }
 
 // The multi-step sequence on the current stream.
+// With obstacles: the first integrate (particle order) with the obstacle
+// contact, then per step the counting sort and a collide that leaves the new
+// velocity at slot i, followed by the obstacle integrate in slot order with
+// the next hash and count; the last collide writes the state back in
+// particle order.
+bool runBatchObstacles(fcdemBatch *b, const CountBuffers &cb, float4 *pos, float4 *vel,
+                       float dt, unsigned steps) {
+  Context &c = ctx();
+  const UmCount count{b->hash, cb.rank, cb.cnt, cb.tileCnt};
+  if (!batchObstacleIntegrate(b->scenes, b->sceneOf, b->radiusFromW, b->maps, b->net, b->skin,
+                              pos, pos, vel, dt, b->n, &count, b->exact))
+    return false;
+  for (unsigned s = 0; s < steps; ++s) {
+    if (!countPipelineSort(c, cb, s == 0 ? nullptr : b->index, pos, vel, b->hash, b->index,
+                           b->sortedPos, b->sortedVel, b->n, b->numCells))
+      return false;
+    const bool last = (s + 1 == steps);
+    CollideOut out;
+    out.posOut = pos;
+    launchCollideBatch(last ? 3 : 4, b->radiusFromW, b->scenes, b->sceneOf, vel, b->sortedPos,
+                       b->sortedVel, b->index, cb.off, b->n, out);
+    if (!last &&
+        !batchObstacleIntegrate(b->scenes, b->sceneOf, b->radiusFromW, b->maps, b->net, b->skin,
+                                b->sortedPos, pos, vel, dt, b->n, &count, b->exact))
+      return false;
+  }
+  return true;
+}
+
 bool runBatch(fcdemBatch *b, float4 *pos, float4 *vel, float dt, unsigned steps) {
   Context &c = ctx();
   CountBuffers cb;
   if (!countBuffersIn(b->countBuf, b->countBytes, b->countCells, b->n, b->numCells, cb))
     return false;
+  if (b->maps) return runBatchObstacles(b, cb, pos, vel, dt, steps);
   if (!countPipelineBeginBatch(b->scenes, b->sceneOf, b->radiusFromW, pos, vel, dt, b->hash,
                                b->n, b->numCells, cb))
     return false;
@@ -113,6 +151,7 @@ fcdemBatch *fcdemBatchCreate(const fcdemBatchScene *scenes, uint numScenes, int 
       d.lo[k] = in.boxLo[k];
       d.hi[k] = in.boxHi[k];
     }
+    d.shape = -1;
     d.cellBase = (unsigned)cellBase;
     d.particleBase = (unsigned)particleBase;
     const float minCell = fminf(p.cellSize[0], fminf(p.cellSize[1], p.cellSize[2]));
@@ -148,6 +187,7 @@ fcdemBatch *fcdemBatchCreate(const fcdemBatchScene *scenes, uint numScenes, int 
   }
   cudaOk(cudaMemcpy(b->scenes, hs.data(), sizeof(BatchScene) * numScenes,
                     cudaMemcpyHostToDevice));
+  b->hostScenes = hs;
   if (b->n)
     cudaOk(cudaMemcpy(b->sceneOf, sceneOf.data(), 4 * (size_t)b->n, cudaMemcpyHostToDevice));
   CountBuffers cb;  // allocate now: recording a graph must not allocate
@@ -160,6 +200,60 @@ fcdemBatch *fcdemBatchCreate(const fcdemBatchScene *scenes, uint numScenes, int 
 }
 
 void fcdemBatchDestroy(fcdemBatch *b) { freeBatch(b); }
+
+void fcdemBatchSetObstacles(fcdemBatch *b, const fcdemDistanceMap *const *maps, uint numMaps,
+                            const int *sceneShape, fcdemSdfNet *net, float skin) {
+  if (!b || (numMaps && (!maps || !sceneShape)) || (net && !(skin >= 0.0f))) {
+    setError(FCDEM_ERR_INVALID_VALUE);
+    return;
+  }
+  for (uint k = 0; k < numMaps; ++k)
+    if (!maps[k]) { setError(FCDEM_ERR_INVALID_VALUE); return; }
+  if (numMaps)
+    for (uint s = 0; s < b->numScenes; ++s)
+      if (sceneShape[s] < -1 || sceneShape[s] >= (int)numMaps) {
+        setError(FCDEM_ERR_INVALID_VALUE);
+        return;
+      }
+  if (!cudaOk(cudaDeviceSynchronize())) return;  // work in flight may read the old ones
+  cudaFree(b->maps);
+  b->maps = nullptr;
+  if (b->exec) {  // a recorded graph holds the old pipeline
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  for (uint s = 0; s < b->numScenes; ++s)
+    b->hostScenes[s].shape = numMaps ? sceneShape[s] : -1;
+  if (!cudaOk(cudaMemcpy(b->scenes, b->hostScenes.data(), sizeof(BatchScene) * b->numScenes,
+                         cudaMemcpyHostToDevice)))
+    return;
+  b->net = numMaps ? net : nullptr;
+  b->skin = skin;
+  if (numMaps == 0) return;
+  std::vector<MapView> hv(numMaps);
+  for (uint k = 0; k < numMaps; ++k) hv[k] = view(maps[k]);
+  if (cudaMalloc(&b->maps, sizeof(MapView) * numMaps) != cudaSuccess ||
+      (!b->exact && cudaMalloc(&b->exact, sizeof(unsigned)) != cudaSuccess)) {
+    cudaGetLastError();
+    cudaFree(b->maps);
+    b->maps = nullptr;
+    setError(FCDEM_ERR_ALLOC);
+    return;
+  }
+  cudaOk(cudaMemcpy(b->maps, hv.data(), sizeof(MapView) * numMaps, cudaMemcpyHostToDevice));
+  cudaOk(cudaMemset(b->exact, 0, sizeof(unsigned)));
+}
+
+unsigned long long fcdemBatchExactQueries(fcdemBatch *b, int reset) {
+  if (!b) { setError(FCDEM_ERR_INVALID_VALUE); return 0; }
+  if (!b->exact) return 0;
+  unsigned v = 0;
+  if (!cudaOk(cudaDeviceSynchronize()) ||
+      !cudaOk(cudaMemcpy(&v, b->exact, sizeof(unsigned), cudaMemcpyDeviceToHost)))
+    return 0;
+  if (reset) cudaOk(cudaMemset(b->exact, 0, sizeof(unsigned)));
+  return v;
+}
 
 uint fcdemBatchNumParticles(const fcdemBatch *b) { return b ? b->n : 0u; }
 uint fcdemBatchNumCells(const fcdemBatch *b) { return b ? b->numCells : 0u; }

@@ -847,6 +847,10 @@ kCollideBatch(const BatchScene *__restrict__ scenes, const unsigned *__restrict_
     out.hashOut[i] = h;
     out.rankOut[i] = atomicAdd(out.cnt + h, 1u);
     countTile(out.tileCnt, h >> 12);
+  } else if (kMode == 4) {
+    // obstacle batches: the new velocity at slot i; the integrate with the
+    // obstacle contact follows in its own kernel
+    newVel[i] = make_float4(nv.x, nv.y, nv.z, 0.0f);
   } else {
     unsigned o = __ldg(index + i);
     if (o >= n) return;
@@ -921,6 +925,12 @@ void launchCollideBatch(int mode, bool radiusFromW, const BatchScene *scenes,
                                                              index, off, n, out, st);
   else if (mode == 2)
     kCollideBatch<2, true><<<blocks, 128, 0, curStream()>>>(scenes, sceneOf, newVel, sp, sv,
+                                                            index, off, n, out, st);
+  else if (mode == 4 && !radiusFromW)
+    kCollideBatch<4, false><<<blocks, 128, 0, curStream()>>>(scenes, sceneOf, newVel, sp, sv,
+                                                             index, off, n, out, st);
+  else if (mode == 4)
+    kCollideBatch<4, true><<<blocks, 128, 0, curStream()>>>(scenes, sceneOf, newVel, sp, sv,
                                                             index, off, n, out, st);
   else if (!radiusFromW)
     kCollideBatch<3, false><<<blocks, 128, 0, curStream()>>>(scenes, sceneOf, newVel, sp, sv,

@@ -90,6 +90,44 @@ kTorusMap(float4 *__restrict__ vert, int vx, int vy, int vz, float3 vmin, float 
   }
 }
 
+// Exact signed distance and closest point of a box with half-extents h whose
+// edges and corners are rounded with radius rr (the box of half-extents
+// h - rr grown by rr), centred at the origin, at every lattice vertex.
+__global__ void __launch_bounds__(256)
+kRoundedBoxMap(float4 *__restrict__ vert, int vx, int vy, int vz, float3 vmin, float cs,
+               float3 h, float rr) {
+  const long long total = (long long)vx * vy * vz;
+  const double in[3] = {(double)h.x - rr, (double)h.y - rr, (double)h.z - rr};
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % vx), j = (int)((t / vx) % vy), k = (int)(t / ((long long)vx * vy));
+    const double p[3] = {(double)vcoord(vmin.x, i, cs), (double)vcoord(vmin.y, j, cs),
+                         (double)vcoord(vmin.z, k, cs)};
+    double c[3], q[3], o2 = 0.0, qmax = -1e300;
+    int kmax = 0;
+    for (int a = 0; a < 3; ++a) {
+      c[a] = fmin(fmax(p[a], -in[a]), in[a]);  // closest point of the inner box
+      q[a] = fabs(p[a]) - in[a];
+      o2 += (p[a] - c[a]) * (p[a] - c[a]);
+      if (q[a] > qmax) {
+        qmax = q[a];
+        kmax = a;
+      }
+    }
+    double d, cp[3];
+    if (o2 > 0.0) {  // outside the inner box: towards its closest point
+      const double o = sqrt(o2);
+      d = o - rr;
+      for (int a = 0; a < 3; ++a) cp[a] = c[a] + rr * (p[a] - c[a]) / o;
+    } else {  // inside it: the nearest flat face
+      d = qmax - rr;
+      for (int a = 0; a < 3; ++a) cp[a] = p[a];
+      cp[kmax] = (p[kmax] < 0.0 ? -1.0 : 1.0) * (in[kmax] + rr);
+    }
+    vert[t] = make_float4((float)d, (float)cp[0], (float)cp[1], (float)cp[2]);
+  }
+}
+
 }  // namespace
 }  // namespace fcdem
 
@@ -184,6 +222,40 @@ fcdemDistanceMap *fcdemDistMapTorus(float majorRadius, float tubeRadius, int cel
                                               cells[2] + 1,
                                               make_float3(vmin[0], vmin[1], vmin[2]), cs,
                                               majorRadius, tubeRadius);
+  launchOk();
+  return m;
+}
+
+fcdemDistanceMap *fcdemDistMapRoundedBox(const float halfExtents[3], float rounding,
+                                         int cellsPerAxis, float margin) {
+  if (!halfExtents || cellsPerAxis < 1 || !(rounding >= 0.0f) || !(margin >= 0.0f) ||
+      !(halfExtents[0] > rounding) || !(halfExtents[1] > rounding) ||
+      !(halfExtents[2] > rounding)) {
+    setError(FCDEM_ERR_INVALID_VALUE);
+    return nullptr;
+  }
+  // cubic cells: the largest axis gets cellsPerAxis cells over
+  // +-(h + margin), the others whole cells covering theirs
+  float ex[3], big = 0.0f;
+  for (int a = 0; a < 3; ++a) {
+    ex[a] = halfExtents[a] + margin;
+    big = std::fmax(big, ex[a]);
+  }
+  const float cs = 2.0f * big / (float)cellsPerAxis;
+  int cells[3];
+  float vmin[3], vmax[3];
+  for (int a = 0; a < 3; ++a) {
+    cells[a] = (int)std::ceil(2.0f * ex[a] / cs);
+    if (cells[a] < 1) cells[a] = 1;
+    vmin[a] = -0.5f * cells[a] * cs;
+    vmax[a] = vmin[a] + cells[a] * cs;
+  }
+  fcdemDistanceMap *m = fcdemDistMapCreate(nullptr, nullptr, vmin, vmax, cs, cells);
+  if (!m) return nullptr;
+  kRoundedBoxMap<<<152 * 8, 256, 0, curStream()>>>(
+      m->vert, cells[0] + 1, cells[1] + 1, cells[2] + 1,
+      make_float3(vmin[0], vmin[1], vmin[2]), cs,
+      make_float3(halfExtents[0], halfExtents[1], halfExtents[2]), rounding);
   launchOk();
   return m;
 }

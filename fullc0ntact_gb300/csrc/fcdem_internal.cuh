@@ -140,7 +140,7 @@ struct BatchScene {
   unsigned cellBase;      // global id of the scene's cell 0
   unsigned particleBase;  // first particle of the scene
   int cull;               // collide may cull cells (see launchCollide)
-  int pad;
+  int shape;              // the scene's obstacle (index into the batch's maps), -1: none
 };
 
 // Batched collide: particles of many scenes in one launch; sceneOf[i] is
@@ -188,6 +188,18 @@ bool umHashCount(const float4 *pos, unsigned n, const KParams &kp, const UmCount
 // nullptr: no obstacle).
 bool mapIntegrate(float4 *pos, float4 *vel, float dt, unsigned n, const KParams &kp,
                   const fcdemDistanceMap *map, const UmCount *count);
+// Batch step with obstacles (fcdem_sdf.cu): for particle / slot i of scene
+// sceneOf[i], the integrate in the scene's box with the contact of its
+// obstacle maps[scenes[.].shape] between the velocity/position update and the
+// box clamp; the map query culled by `net` where it predicts more than
+// `skin` (net == nullptr: every in-box particle queries the map).  Reads
+// inPos[i], vel[i]; writes pos[i], vel[i] and, with count, the next hash and
+// count.  exact (optional) counts the exact queries.
+struct MapView;
+bool batchObstacleIntegrate(const BatchScene *scenes, const unsigned *sceneOf, bool radiusFromW,
+                            const MapView *maps, fcdemSdfNet *net, float skin,
+                            const float4 *inPos, float4 *pos, float4 *vel, float dt,
+                            unsigned n, const UmCount *count, unsigned *exact);
 // The same with the neural-SDF culling of the map query (fcdem_sdf.cu).
 bool sdfIntegrate(fcdemSdfNet *net, float4 *pos, float4 *vel, float dt, unsigned n,
                   const KParams &kp, const fcdemDistanceMap *map, float skin, unsigned *exact,

@@ -673,6 +673,83 @@ kIntegrateSdf(float4 *__restrict__ pos, float4 *__restrict__ vel, float dt, unsi
   sdfTileTeardown<H, L>(sm);
 }
 
+// integrateOneBox's clamp to the scene box, same faces in the same order,
+// the roundings spelled out.
+__device__ __forceinline__ void boxClamp(float3 &p, float3 &v, float r, float bd,
+                                         const float *lo, const float *hi) {
+  if (p.x > hi[0] - r) { p.x = hi[0] - r; v.x = __fmul_rn(v.x, bd); }
+  if (p.x < lo[0] + r) { p.x = lo[0] + r; v.x = __fmul_rn(v.x, bd); }
+  if (p.y > hi[1] - r) { p.y = hi[1] - r; v.y = __fmul_rn(v.y, bd); }
+  if (p.z > hi[2] - r) { p.z = hi[2] - r; v.z = __fmul_rn(v.z, bd); }
+  if (p.z < lo[2] + r) { p.z = lo[2] + r; v.z = __fmul_rn(v.z, bd); }
+  if (p.y < lo[1] + r) { p.y = lo[1] + r; v.y = __fmul_rn(v.y, bd); }
+}
+
+// Batch integrate with obstacles: particle / slot i belongs to scene
+// sceneOf[i]; the velocity and position update, the contact of the scene's
+// obstacle map (checkDistMap), the clamp to the scene's box, and with
+// doCount the next global cell id and count.  kNet: a tile of 128 with a
+// particle in its obstacle's map box runs the network (the scene's shape as
+// the one-hot code) and only particles predicted within `skin` query the map.
+template <int H, int L, bool kNet, bool kW>
+__global__ void __launch_bounds__(128)
+kBatchObstacle(const BatchScene *__restrict__ scenes, const unsigned *__restrict__ sceneOf,
+               const MapView *__restrict__ maps, SdfView net, float skin,
+               const float4 *__restrict__ inPos, float4 *__restrict__ pos,
+               float4 *__restrict__ vel, float dt, unsigned n, UmCount count, int doCount,
+               unsigned *exact, unsigned *status) {
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  SdfTileSmem<H, L> &sm = *reinterpret_cast<SdfTileSmem<H, L> *>(smraw);
+  if (kNet) sdfTileSetup<H, L>(sm, net);
+  unsigned phase = 0;
+  const unsigned tiles = (n + 127) / 128;
+  for (unsigned tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const unsigned i = tile * 128 + threadIdx.x;
+    const bool valid = i < n;
+    const BatchScene *S = valid ? scenes + __ldg(sceneOf + i) : scenes;
+    const SimParams &P = S->p;
+    float4 p4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), v4 = p4;
+    if (valid) {
+      p4 = inPos[i];
+      v4 = vel[i];
+    }
+    float3 p = make_float3(p4.x, p4.y, p4.z), v = make_float3(v4.x, v4.y, v4.z);
+    const float r = kW ? p4.w : P.particleRadius;
+    umAdvance(p, v, dt, P);
+    const int shape = valid ? S->shape : -1;
+    MapView M{};
+    if (shape >= 0) M = maps[shape];
+    const bool inBox = shape >= 0 && inMapBox(M, p);
+    float dPred = 0.0f;
+    if (kNet) {
+      if (__syncthreads_or(inBox) &&
+          !sdfTileForward<H, L>(sm, net, (p.x - net.shift[0]) * net.scale[0],
+                                (p.y - net.shift[1]) * net.scale[1],
+                                (p.z - net.shift[2]) * net.scale[2], shape, phase, dPred)) {
+        if (threadIdx.x == 0) atomicOr(status, (unsigned)kStatusTimeout);
+        break;
+      }
+    }
+    if (!valid) continue;
+    const bool test = inBox && (!kNet || !(dPred > skin));
+    if (test) {
+      if (exact) atomicAdd(exact, 1u);
+      checkDistMap(M, r, P.boundaryDamping, p, v);
+    }
+    boxClamp(p, v, r, P.boundaryDamping, S->lo, S->hi);
+    pos[i] = make_float4(p.x, p.y, p.z, p4.w);
+    vel[i] = make_float4(v.x, v.y, v.z, v4.w);
+    if (doCount) {
+      const int3 gp = gridPos(p.x, p.y, p.z, P);
+      const unsigned h = S->cellBase + gridHash(gp.x, gp.y, gp.z, P);
+      count.hash[i] = h;
+      count.rank[i] = atomicAdd(count.cnt + h, 1u);
+      countTile(count.tileCnt, h >> 12);
+    }
+  }
+  if (kNet) sdfTileTeardown<H, L>(sm);
+}
+
 // Hidden-layer weights, FP32 [out][in], to the BF16 B-operand tiles.
 __global__ void __launch_bounds__(256)
 kSdfPackBf16(const float *__restrict__ p, SdfLayout ly, __nv_bfloat16 *__restrict__ w16) {
@@ -857,10 +934,62 @@ bool launchIntegrateSdf(fcdemSdfNet *net, float4 *pos, float4 *vel, float dt, un
   return launchOk();
 }
 
+template <int H, int L, bool kNet, bool kW>
+bool launchBatchObstacle(fcdemSdfNet *net, const BatchScene *scenes, const unsigned *sceneOf,
+                         const MapView *maps, float skin, const float4 *inPos, float4 *pos,
+                         float4 *vel, float dt, unsigned n, const UmCount *count,
+                         unsigned *exact) {
+  unsigned grid = (n + 127) / 128;
+  size_t smem = 0;
+  SdfView v{};
+  if (kNet) {
+    smem = tileSmemBytes<H, L>();
+    cudaFuncSetAttribute(kBatchObstacle<H, L, kNet, kW>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (grid > 152u * sdfCtasPerSm<H, L>()) grid = 152u * sdfCtasPerSm<H, L>();
+    v = sdfView(net);
+  }
+  kBatchObstacle<H, L, kNet, kW><<<grid, 128, smem, curStream()>>>(
+      scenes, sceneOf, maps, v, skin, inPos, pos, vel, dt, n, count ? *count : UmCount{},
+      count ? 1 : 0, exact, ctx().dStatus);
+  return launchOk();
+}
+
 }  // namespace
 }  // namespace fcdem
 
 namespace fcdem {
+
+bool batchObstacleIntegrate(const BatchScene *scenes, const unsigned *sceneOf, bool radiusFromW,
+                            const MapView *maps, fcdemSdfNet *net, float skin,
+                            const float4 *inPos, float4 *pos, float4 *vel, float dt,
+                            unsigned n, const UmCount *count, unsigned *exact) {
+  if (n == 0) return true;
+  if (!net) {
+    return radiusFromW
+               ? launchBatchObstacle<64, 3, false, true>(net, scenes, sceneOf, maps, skin, inPos,
+                                                         pos, vel, dt, n, count, exact)
+               : launchBatchObstacle<64, 3, false, false>(net, scenes, sceneOf, maps, skin,
+                                                          inPos, pos, vel, dt, n, count, exact);
+  }
+  if (!packWeights(net)) return false;
+  const int H = net->lay.H, L = net->lay.L;
+#define FCDEM_BATCH_OBST(HH, LL)                                                             \
+  if (H == HH && L == LL)                                                                    \
+    return radiusFromW ? launchBatchObstacle<HH, LL, true, true>(net, scenes, sceneOf, maps, \
+                                                                 skin, inPos, pos, vel, dt,  \
+                                                                 n, count, exact)            \
+                       : launchBatchObstacle<HH, LL, true, false>(                           \
+                             net, scenes, sceneOf, maps, skin, inPos, pos, vel, dt, n,       \
+                             count, exact);
+  FCDEM_BATCH_OBST(64, 3)
+  FCDEM_BATCH_OBST(64, 2)
+  FCDEM_BATCH_OBST(128, 2)
+  FCDEM_BATCH_OBST(128, 3)
+#undef FCDEM_BATCH_OBST
+  setError(FCDEM_ERR_INVALID_VALUE);
+  return false;
+}
 
 bool sdfIntegrate(fcdemSdfNet *net, float4 *pos, float4 *vel, float dt, unsigned n,
                   const KParams &kp, const fcdemDistanceMap *map, float skin, unsigned *exact,

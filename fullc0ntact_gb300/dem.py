@@ -254,6 +254,12 @@ class DistanceMap:
         return cls(h)
 
     @classmethod
+    def rounded_box(cls, half_extents, rounding=0.02, cells_per_axis=128, margin=0.05):
+        h = lib.fcdemDistMapRoundedBox(_f3(half_extents), rounding, cells_per_axis, margin)
+        check("fcdemDistMapRoundedBox")
+        return cls(h)
+
+    @classmethod
     def torus(cls, major_radius=0.3, tube_radius=0.1, cells_per_axis=128, margin=0.05):
         h = lib.fcdemDistMapTorus(major_radius, tube_radius, cells_per_axis, margin)
         check("fcdemDistMapTorus")
@@ -360,6 +366,11 @@ _B_SIGS = {
     "fcdemBatchNumCells": (C.c_uint, [C.c_void_p]),
     "fcdemBatchUpdate": (None, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_uint,
                                 C.c_int]),
+    "fcdemBatchSetObstacles": (None, [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint,
+                                      C.POINTER(C.c_int), C.c_void_p, C.c_float]),
+    "fcdemBatchExactQueries": (C.c_ulonglong, [C.c_void_p, C.c_int]),
+    "fcdemDistMapRoundedBox": (C.c_void_p, [C.POINTER(C.c_float), C.c_float, C.c_int,
+                                            C.c_float]),
 }
 for _n, (_r, _a) in _B_SIGS.items():
     getattr(lib, _n).restype = _r
@@ -401,6 +412,22 @@ class Batch:
     def update(self, steps: int = 1, dt: float | None = None, graph: bool = True) -> None:
         lib.fcdemBatchUpdate(self._h, _p(self.pos), _p(self.vel),
                              self.dt if dt is None else dt, steps, int(graph))
+
+    def set_obstacles(self, maps: list, scene_shape, net=None, skin: float = 0.0) -> None:
+        """Scene s gets obstacle maps[scene_shape[s]] (-1: none); with `net`
+        (an sdf.SdfNet) the map query is culled above `skin`."""
+        self._maps = list(maps)  # keep them alive while the batch uses them
+        self._net = net
+        hs = (C.c_void_p * max(len(maps), 1))(*[m.handle for m in maps])
+        sh = (C.c_int * len(self.sizes))(*[int(x) for x in scene_shape])
+        lib.fcdemBatchSetObstacles(self._h, hs, len(maps), sh,
+                                   net.handle if net is not None else None, skin)
+        check("fcdemBatchSetObstacles")
+
+    def exact_queries(self, reset: bool = False) -> int:
+        v = int(lib.fcdemBatchExactQueries(self._h, int(reset)))
+        check("fcdemBatchExactQueries")
+        return v
 
     def split(self, t: torch.Tensor) -> list:
         return list(torch.split(t, self.sizes))

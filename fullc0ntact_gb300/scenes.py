@@ -183,3 +183,65 @@ def batch_config3(num_scenes: int = 512, n_min: int = 1024, n_max: int = 65536,
     rng = np.random.default_rng(seed)
     sizes = np.exp(rng.uniform(np.log(n_min), np.log(n_max), num_scenes)).astype(np.int64)
     return [batch_scene(int(n), seed * 100003 + k) for k, n in enumerate(sizes)]
+
+
+def obstacle_set(num: int = 8, seed: int = 41) -> list:
+    """The procedural obstacles of the batched neural-SDF workload: half tori
+    (major radius U[0.2, 0.35], tube radius U[0.05, 0.12]) and half rounded
+    boxes (half-extents U[0.1, 0.3] per axis, rounding 0.02), seeded; each a
+    dict kind/params, centred at the origin."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(num):
+        if k % 2 == 0:
+            out.append(dict(kind="torus", R=float(rng.uniform(0.2, 0.35)),
+                            r=float(rng.uniform(0.05, 0.12))))
+        else:
+            out.append(dict(kind="box", h=[float(x) for x in rng.uniform(0.1, 0.3, 3)],
+                            rounding=0.02))
+    return out
+
+
+def obstacle_top(ob: dict) -> float:
+    return ob["r"] if ob["kind"] == "torus" else ob["h"][2]
+
+
+def obstacle_scene(n: int, ob: dict, seed: int, r_min: float = 1.0 / 512.0,
+                   r_max: float = 1.0 / 256.0) -> dict:
+    """One scene of the batched neural-SDF workload: n spheres with radii
+    U[r_min, r_max] on a jittered lattice (spacing 2.05 r_max, at most
+    120 x 120 columns) starting one diameter above the obstacle's top,
+    falling (gravity -3e-4 along z) onto it inside the box [-0.5, 0.5]^3;
+    128^3 grid cells of one max diameter; config0 contact parameters."""
+    rng = np.random.default_rng(seed)
+    sp = 2.05 * r_max
+    nx = ny = min(120, max(1, int(np.ceil(np.sqrt(n)))))
+    k = np.arange(n)
+    ix, iy, iz = k % nx, (k // nx) % ny, k // (nx * ny)
+    pos = np.zeros((n, 4), np.float32)
+    pos[:, 0] = (ix - (nx - 1) / 2.0) * sp
+    pos[:, 1] = (iy - (ny - 1) / 2.0) * sp
+    pos[:, 2] = obstacle_top(ob) + 2.0 * r_max + iz * sp
+    pos[:, :3] += rng.uniform(-0.02 * r_max, 0.02 * r_max, (n, 3))
+    pos[:, 3] = rng.uniform(r_min, r_max, n)
+    vel = np.zeros((n, 4), np.float32)
+    vel[:, :3] = rng.uniform(-0.001, 0.001, (n, 3))
+    p = make_params(n, (128, 128, 128), particle_radius=r_max, cell_size=2.0 * r_max,
+                    world_origin=(-0.5, -0.5, -0.5), gravity=(0.0, 0.0, -3e-4),
+                    collider_pos=(10.0, 10.0, 10.0), collider_radius=0.0)
+    return dict(name=f"obstacle-scene-{n}", pos=pos, vel=vel, params=p, radius_from_w=True,
+                dt=0.5, box_lo=np.array([-0.5] * 3, np.float32),
+                box_hi=np.array([0.5] * 3, np.float32))
+
+
+def batch_config4(num_scenes: int = 128, n_min: int = 4096, n_max: int = 262144,
+                  seed: int = 4, num_shapes: int = 8):
+    """Batched DEM with obstacles: scene sizes log-uniform in [n_min, n_max]
+    (seeded), scene s over obstacle s % num_shapes.  Returns (scenes,
+    obstacles, scene_shape)."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(n_min), np.log(n_max), num_scenes)).astype(np.int64)
+    obs = obstacle_set(num_shapes)
+    shape = [k % num_shapes for k in range(num_scenes)]
+    scs = [obstacle_scene(int(n), obs[shape[k]], seed * 100003 + k) for k, n in enumerate(sizes)]
+    return scs, obs, shape

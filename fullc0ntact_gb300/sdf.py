@@ -145,3 +145,40 @@ def um_integrate_system_sdf(pos, vel, dt: float, n: int, dmap: DistanceMap, net:
                             skin: float, exact_counter: torch.Tensor | None = None) -> None:
     lib.fcdemUM_integrateSystemSdf(_p(pos), _p(vel), dt, n, dmap.handle, net.handle, skin,
                                    _opt(exact_counter))
+
+
+def obstacle_maps(obstacles: list, cells_per_axis: int = 128, margin: float = 0.05) -> list:
+    """DistanceMap of each obstacle of scenes.obstacle_set."""
+    from .dem import DistanceMap
+    out = []
+    for ob in obstacles:
+        if ob["kind"] == "torus":
+            out.append(DistanceMap.torus(ob["R"], ob["r"], cells_per_axis, margin))
+        else:
+            out.append(DistanceMap.rounded_box(ob["h"], ob["rounding"], cells_per_axis, margin))
+    return out
+
+
+def shape_net(maps: list, samples_per_map: int = 500_000, hidden: int = 128, layers: int = 2,
+              epochs: int = 20, batch: int = 2048, lr: float = 3e-3, band: float = 0.02,
+              seed: int = 9):
+    """A shape-conditioned network (3 + len(maps) inputs) trained on samples
+    of every map, each with its shape code; inputs and outputs normalised by
+    the largest half-extent over the maps.  Returns (net, final loss)."""
+    lo = np.min([m.vmin for m in maps], axis=0)
+    hi = np.max([m.vmax for m in maps], axis=0)
+    half = float(np.max(np.maximum(np.abs(lo), np.abs(hi))))
+    net = SdfNet(3 + len(maps), hidden, layers, seed=seed)
+    net.set_normalization([0.0, 0.0, 0.0], [1.0 / half] * 3, half)
+    parts, shapes = [], []
+    for k, m in enumerate(maps):
+        s_k, sh_k = samples(m, samples_per_map, 0.6, 0.05, seed=seed * 131 + k, shape=k)
+        parts.append(s_k)
+        shapes.append(sh_k)
+    s = torch.cat(parts)
+    sh = torch.cat(shapes)
+    g = torch.Generator(device=s.device).manual_seed(seed)
+    perm = torch.randperm(s.shape[0], device=s.device, generator=g)
+    s, sh = s[perm].contiguous(), sh[perm].contiguous()
+    loss = net.train(s, sh, epochs=epochs, batch=batch, lr=lr, band=band)
+    return net, loss

@@ -257,6 +257,12 @@ fcdemDistanceMap *fcdemDistMapCreate(const float *distance, const float *contact
  * +-(r + margin) (the cubic-cell rule of distancemap.cpp:180-229). */
 fcdemDistanceMap *fcdemDistMapTorus(float majorRadius, float tubeRadius, int cellsPerAxis,
                                     float margin);
+/* A map of a box with half-extents halfExtents whose edges and corners are
+ * rounded with radius `rounding`, centred at the origin: cubic cells, the
+ * largest axis cut into cellsPerAxis cells over +-(h + margin).  Exact
+ * signed distance and closest point at every vertex. */
+fcdemDistanceMap *fcdemDistMapRoundedBox(const float halfExtents[3], float rounding,
+                                         int cellsPerAxis, float margin);
 void fcdemDistMapDestroy(fcdemDistanceMap *map);
 void fcdemDistMapGeometry(const fcdemDistanceMap *map, float vmin[3], float vmax[3],
                           float *cellSize, int cells[3]);
@@ -371,6 +377,18 @@ typedef struct fcdemBatch fcdemBatch;
 /* radiusFromW applies to every scene (fcdemSetRadiusMode). */
 fcdemBatch *fcdemBatchCreate(const fcdemBatchScene *scenes, uint numScenes, int radiusFromW);
 void fcdemBatchDestroy(fcdemBatch *batch);
+/* Obstacles (no counterpart in the reference): scene s gets the distance map
+ * maps[sceneShape[s]] (-1: none), centred in its coordinates.  Each integrate
+ * of the batch then applies checkDistMap (boundaries.cuh:38-63) between the
+ * velocity/position update and the box clamp.  With net, the map query is
+ * culled where the network (shape code = sceneShape[s]) predicts a distance
+ * above `skin`.  The maps and the network must outlive their use; numMaps 0
+ * removes the obstacles.  Synchronises. */
+void fcdemBatchSetObstacles(fcdemBatch *batch, const fcdemDistanceMap *const *maps,
+                            uint numMaps, const int *sceneShape, fcdemSdfNet *net, float skin);
+/* Exact map queries made by the batch's integrates since the last reset
+ * (synchronises); reset != 0 clears the count. */
+unsigned long long fcdemBatchExactQueries(fcdemBatch *batch, int reset);
 uint fcdemBatchNumParticles(const fcdemBatch *batch);
 uint fcdemBatchNumCells(const fcdemBatch *batch);
 /* `steps` updates of every scene, each stage one launch over all particles.

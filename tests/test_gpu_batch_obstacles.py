@@ -1,0 +1,91 @@
+"""Batches with obstacles (config-4 style): the rounded-box map generator
+against the analytic rounded box; a batch with one obstacle map per scene
+gives the same state as each scene stepped alone; the shape-conditioned
+network (11 -> 128 -> 128 -> 1), judged per shape by the exact maps, culls
+the map queries without changing any result."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _rounded_box_sdf(p, h, rr):
+    inner = np.asarray(h, np.float64) - rr
+    q = np.abs(p) - inner
+    outside = np.linalg.norm(np.maximum(q, 0.0), axis=1)
+    inside = np.minimum(q.max(axis=1), 0.0)
+    return outside + inside - rr
+
+
+def test_rounded_box_generator_matches_analytic():
+    from fullc0ntact_gb300 import dem
+    from oracle import oracle as O
+    h, rr = [0.12, 0.27, 0.2], 0.02
+    m = dem.DistanceMap.rounded_box(h, rr, 64, 0.05)
+    v = m.vertices()
+    coords = O.lattice_coords(m.vmin, m.cell_size, m.cells).astype(np.float64)
+    sd = _rounded_box_sdf(coords, h, rr)
+    assert np.abs(v[:, 0] - sd).max() <= 1e-6
+    cp = v[:, 1:].astype(np.float64)
+    assert np.abs(_rounded_box_sdf(cp, h, rr)).max() <= 2e-6  # contact points on the surface
+    dd = np.linalg.norm(coords - cp, axis=1)  # |distance| = |vertex - contact point|
+    assert np.abs(np.abs(v[:, 0]) - dd).max() <= 2e-6
+
+
+def _small_config4(num_scenes=6, n_min=3000, n_max=20000, seed=5):
+    from fullc0ntact_gb300 import scenes
+    return scenes.batch_config4(num_scenes, n_min, n_max, seed=seed, num_shapes=4)
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_obstacle_batch_equals_each_scene_alone(graph):
+    from fullc0ntact_gb300 import dem, sdf
+    scs, obs, shape = _small_config4()
+    maps = sdf.obstacle_maps(obs, 64)
+    b = dem.Batch(scs)
+    b.set_obstacles(maps, shape)
+    steps = 25
+    b.update(steps, graph=graph)
+    dem.check("batch")
+    assert b.exact_queries() > 0  # the spheres reach their obstacles
+    for k, sc in enumerate(scs):
+        one = dem.Batch([sc])
+        one.set_obstacles(maps, [shape[k]])
+        one.update(steps, graph=False)
+        dem.check("scene")
+        for x, y in ((b.split(b.pos)[k], one.pos), (b.split(b.vel)[k], one.vel)):
+            np.testing.assert_array_equal(x.cpu().numpy().view(np.uint32),
+                                          y.cpu().numpy().view(np.uint32))
+
+
+def test_shape_network_judged_by_maps_and_culling_is_exact():
+    from fullc0ntact_gb300 import dem, sdf
+    scs, obs, shape = _small_config4(num_scenes=8, seed=6)
+    maps = sdf.obstacle_maps(obs, 128)
+    net, loss = sdf.shape_net(maps, samples_per_map=400_000, epochs=20)
+    print("shape net loss", loss)
+    r_max = 1.0 / 256.0
+    skin = 2.0 * r_max
+    for k, m in enumerate(maps):
+        val, sh = sdf.samples(m, 200_000, 0.5, 0.03, seed=500 + k, shape=k)
+        pred = net.infer(val, sh)
+        d = val[:, 3]
+        near = d.abs() < 0.02
+        print(k, "max err near", float((pred - d)[near].abs().max()),
+              "bad", int(((d < r_max) & (pred > skin)).sum()))
+        assert int(((d < r_max) & (pred > skin)).sum()) == 0, k
+        assert float((pred - d)[near].abs().max()) < r_max, k
+    a, b = dem.Batch(scs), dem.Batch(scs)
+    a.set_obstacles(maps, shape)
+    b.set_obstacles(maps, shape, net=net, skin=skin)
+    steps = 40
+    a.update(steps, graph=True)
+    b.update(steps, graph=True)
+    dem.check("batch neural")
+    np.testing.assert_array_equal(a.pos.cpu().numpy().view(np.uint32),
+                                  b.pos.cpu().numpy().view(np.uint32))
+    np.testing.assert_array_equal(a.vel.cpu().numpy().view(np.uint32),
+                                  b.vel.cpu().numpy().view(np.uint32))
+    ea, eb = a.exact_queries(), b.exact_queries()
+    print("exact queries exact/neural", ea, eb)
+    assert 0 < eb < 0.5 * ea, (ea, eb)
