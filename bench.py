@@ -65,6 +65,10 @@ def parse():
                     help="skip the torus-obstacle (distance map / neural SDF) measurement")
     ap.add_argument("--config2-n", type=int, default=1048576)
     ap.add_argument("--config2-steps", type=int, default=200)
+    ap.add_argument("--no-config4", action="store_true",
+                    help="skip the batched scenes with obstacles and the shape network")
+    ap.add_argument("--config4-scenes", type=int, default=128)
+    ap.add_argument("--config4-steps", type=int, default=500)
     ap.add_argument("--batch-scenes", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=20)
     return ap.parse_args()
@@ -357,6 +361,102 @@ def measure_config2(n: int, steps: int, dev: int) -> dict:
                                       "frac": tc_flop / (infer_ms / 1e3) / 1e12 / peak_tf}}
 
 
+def measure_config4(num_scenes: int, steps: int, dev: int) -> dict:
+    """Batched + neural SDF: scenes with sizes log-uniform in [4096, 262144],
+    each over one of 8 procedural obstacles (128-cell maps); one
+    shape-conditioned network (11 -> 128 -> 128 -> 1) trained on samples of
+    all maps.  Timed over the same job from the same initial state: the
+    whole batch replayed from a CUDA graph with the network culling the map
+    query; the batch with exact queries; each scene stepped alone with exact
+    queries (the plain step)."""
+    import torch
+    from fullc0ntact_gb300 import dem, scenes, sdf
+    scs, obs, shape = scenes.batch_config4(num_scenes)
+    n_total = sum(s["pos"].shape[0] for s in scs)
+    maps = sdf.obstacle_maps(obs, 128)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    net, loss = sdf.shape_net(maps)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    r_max = 1.0 / 256.0
+    skin = 2.0 * r_max
+    worst_err, bad = 0.0, 0
+    for k, m in enumerate(maps):
+        val, sh = sdf.samples(m, 200_000, 0.5, 0.03, seed=700 + k, shape=k)
+        pred = net.infer(val, sh)
+        d = val[:, 3]
+        bad += int(((d < r_max) & (pred > skin)).sum())
+        near = d.abs() < 0.02
+        worst_err = max(worst_err, float((pred - d)[near].abs().max()))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    pos0 = torch.from_numpy(np.concatenate([s["pos"] for s in scs]))
+    vel0 = torch.from_numpy(np.concatenate([s["vel"] for s in scs]))
+
+    def timed_batch(use_net):
+        b = dem.Batch(scs, f"cuda:{dev}")
+        b.set_obstacles(maps, shape, net if use_net else None, skin)
+        b.update(steps, graph=True)  # records the graph (and warms up)
+        b.pos.copy_(pos0)
+        b.vel.copy_(vel0)
+        b.exact_queries(reset=True)
+        torch.cuda.synchronize()
+        e0.record()
+        b.update(steps, graph=True)
+        e1.record()
+        torch.cuda.synchronize()
+        dem.check("config4 batch")
+        return b, e0.elapsed_time(e1), b.exact_queries()
+
+    bn, ms_n, ex_n = timed_batch(True)
+    bp, ms_p, ex_p = timed_batch(False)
+    same = (torch.equal(bn.pos.view(torch.int32), bp.pos.view(torch.int32)) and
+            torch.equal(bn.vel.view(torch.int32), bp.vel.view(torch.int32)))
+    del bn, bp
+    torch.cuda.empty_cache()
+    singles = []
+    for k, sc in enumerate(scs):
+        one = dem.Batch([sc], f"cuda:{dev}")
+        one.set_obstacles(maps, [shape[k]])
+        one.update(1, graph=False)
+        one.pos.copy_(torch.from_numpy(sc["pos"]))
+        one.vel.copy_(torch.from_numpy(sc["vel"]))
+        singles.append(one)
+    torch.cuda.synchronize()
+    e0.record()
+    for one in singles:
+        one.update(steps, graph=False)
+    e1.record()
+    torch.cuda.synchronize()
+    dem.check("config4 per scene")
+    ms_s = e0.elapsed_time(e1)
+    del singles
+    torch.cuda.empty_cache()
+
+    def val_of(ms):
+        return n_total * steps / (ms / 1e3)
+
+    sizes = [s["pos"].shape[0] for s in scs]
+    return {"workload": f"{num_scenes} scenes, sizes log-uniform in [4096, 262144], radii "
+                        "U[1/512, 1/256] falling onto one of 8 obstacles (tori, rounded boxes; "
+                        f"128-cell maps) in [-0.5, 0.5]^3, 128^3 cells each, {steps} steps",
+            "n_total": n_total, "scene_min": int(min(sizes)), "scene_max": int(max(sizes)),
+            "steps": steps, "unit": UNIT,
+            "batched_neural_graph": {"value": val_of(ms_n), "ms_per_step": ms_n / steps,
+                                     "exact_map_queries_per_step": ex_n / steps},
+            "batched_exact_graph": {"value": val_of(ms_p), "ms_per_step": ms_p / steps,
+                                    "exact_map_queries_per_step": ex_p / steps},
+            "plain_per_scene_exact": {"value": val_of(ms_s), "ms_per_step": ms_s / steps},
+            "speedup_vs_plain": ms_s / ms_n,
+            "network_effect_in_batch": ms_p / ms_n,
+            "equal_final_state_neural_vs_exact": bool(same),
+            "network": {"layers": "11-128-128-1 SiLU (8 one-hot shape codes)",
+                        "params": net.num_params, "train_samples": 500_000 * len(maps),
+                        "epochs": 40, "train_s": train_s, "final_loss": loss,
+                        "judge": {"touching_points_predicted_above_skin": bad,
+                                  "max_abs_err_within_0.02": worst_err}}}
+
+
 def cpu_baseline(sc: dict, steps: int) -> dict:
     """The oracle (C restatement of the reference step) on this host's cores:
     `steps` full updates of the same scene."""
@@ -565,6 +665,11 @@ def run_ours(args):
         config2 = measure_config2(args.config2_n, args.config2_steps, dev)
         torch.cuda.empty_cache()
 
+    config4 = None
+    if not args.no_config4:
+        config4 = measure_config4(args.config4_scenes, args.config4_steps, dev)
+        torch.cuda.empty_cache()
+
     batched = None
     if not args.no_batched:
         del ds  # free the large scene's arrays first
@@ -601,6 +706,7 @@ def run_ours(args):
             "final_cells": final_cells,
             "batched": batched,
             "config2": config2,
+            "config4": config4,
             "clocks": clk,
             "cpu_baseline": cpu,
         }

@@ -160,7 +160,7 @@ def obstacle_maps(obstacles: list, cells_per_axis: int = 128, margin: float = 0.
 
 
 def shape_net(maps: list, samples_per_map: int = 500_000, hidden: int = 128, layers: int = 2,
-              epochs: int = 20, batch: int = 2048, lr: float = 3e-3, band: float = 0.02,
+              epochs: int = 40, batch: int = 2048, lr: float = 5e-3, band: float = 0.02,
               seed: int = 9):
     """A shape-conditioned network (3 + len(maps) inputs) trained on samples
     of every map, each with its shape code; inputs and outputs normalised by
