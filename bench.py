@@ -380,7 +380,7 @@ def measure_config4(num_scenes: int, steps: int, dev: int) -> dict:
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
     r_max = 1.0 / 256.0
-    skin = 2.0 * r_max
+    skin, p_max = sdf.calibrate_skin(net, maps, r_max, seed=300)
     worst_err, bad = 0.0, 0
     for k, m in enumerate(maps):
         val, sh = sdf.samples(m, 200_000, 0.5, 0.03, seed=700 + k, shape=k)
@@ -453,6 +453,8 @@ def measure_config4(num_scenes: int, steps: int, dev: int) -> dict:
             "network": {"layers": "11-128-128-1 SiLU (8 one-hot shape codes)",
                         "params": net.num_params, "train_samples": 500_000 * len(maps),
                         "epochs": 40, "train_s": train_s, "final_loss": loss,
+                        "skin": skin, "skin_radii": skin / r_max,
+                        "max_prediction_at_touching_points": p_max,
                         "judge": {"touching_points_predicted_above_skin": bad,
                                   "max_abs_err_within_0.02": worst_err}}}
 

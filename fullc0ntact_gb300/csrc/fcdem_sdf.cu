@@ -79,10 +79,19 @@ struct SdfView {
 
 __device__ __forceinline__ float sigm(float z) { return 1.0f / (1.0f + expf(-z)); }
 __device__ __forceinline__ float silu(float z) { return z * sigm(z); }
-// Inference SiLU: fast exponential and division (a few ulp of FP32, far
-// below the bf16 rounding of the activations it feeds).
+// Inference SiLU: silu(z) = h + h tanh(h) with h = z / 2, the hardware
+// tanh approximation (one special-function op; relative error about 2^-11,
+// near the bf16 rounding of the activations it feeds).  The culling
+// threshold is calibrated on this arithmetic (the prediction the kernels
+// make), so its error is part of what the exact map judges.
+__device__ __forceinline__ float tanhApprox(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
 __device__ __forceinline__ float siluFast(float z) {
-  return z * __fdividef(1.0f, 1.0f + __expf(-z));
+  const float h = 0.5f * z;
+  return fmaf(h, tanhApprox(h), h);
 }
 __device__ __forceinline__ float dsilu(float z) {
   const float s = sigm(z);

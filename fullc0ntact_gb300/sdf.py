@@ -182,3 +182,23 @@ def shape_net(maps: list, samples_per_map: int = 500_000, hidden: int = 128, lay
     s, sh = s[perm].contiguous(), sh[perm].contiguous()
     loss = net.train(s, sh, epochs=epochs, batch=batch, lr=lr, band=band)
     return net, loss
+
+
+def calibrate_skin(net: SdfNet, maps: list, radius: float, samples_per_map: int = 200_000,
+                   seed: int = 300, shaped: bool = True) -> tuple:
+    """The culling threshold, judged by the exact maps: on held-out samples
+    of every map, p_max = the largest prediction at a point the map puts
+    within one radius of the surface (or inside the obstacle), the value that
+    must not be culled.  The skin is max(2 radius, p_max + 0.25 (p_max -
+    radius)).  Returns (skin, p_max)."""
+    p_max = -1e30
+    for k, m in enumerate(maps):
+        if shaped:
+            val, sh = samples(m, samples_per_map, 0.5, 0.03, seed=seed + k, shape=k)
+        else:
+            val, sh = samples(m, samples_per_map, 0.5, 0.03, seed=seed + k), None
+        pred = net.infer(val, sh)
+        touching = val[:, 3] < radius
+        if bool(touching.any()):
+            p_max = max(p_max, float(pred[touching].max()))
+    return max(2.0 * radius, p_max + 0.25 * max(p_max - radius, 0.0)), p_max

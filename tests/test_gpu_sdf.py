@@ -112,9 +112,10 @@ def test_fp32_forward_matches_torch(cfg):
 
 @pytest.mark.parametrize("cfg", CONFIGS)
 def test_tensor_core_inference_matches_bf16_reference(cfg):
-    """kSdfInfer (tcgen05.mma, BF16 operands, FP32 accumulation in TMEM)
-    against the PyTorch fp32 forward with the same operands rounded to bf16;
-    ragged tail (n not a multiple of the 128-point tile)."""
+    """kSdfInfer (tcgen05.mma, BF16 operands, FP32 accumulation in TMEM,
+    approximate-tanh SiLU) against the PyTorch fp32 forward with the same
+    operands rounded to bf16; ragged tail (n not a multiple of the 128-point
+    tile)."""
     from fullc0ntact_gb300 import sdf
     dmap = _torus()
     net = _net(*cfg, dmap, jitter=0.05)
@@ -129,13 +130,13 @@ def test_tensor_core_inference_matches_bf16_reference(cfg):
     q999 = float(torch.quantile(diff[:100_000], 0.999))
     print(f"cfg {cfg}: max {float(diff.max()):.3e} mean {float(diff.mean()):.3e} "
           f"q99.9 {q999:.3e} scale {scale:.3e}")
-    # The FP32 sums run in another order than PyTorch's, so an activation
-    # near a bf16 rounding boundary can round the other way (one bf16 ulp,
-    # 2^-8 relative) and move that prediction; most predictions agree to
-    # FP32 accumulation noise.
-    assert float(diff.max()) <= 5e-3 * scale, (float(diff.max()), scale)
-    assert q999 <= 5e-4 * scale, (q999, scale)
-    assert float(diff.mean()) <= 2e-5 * scale
+    # The kernel's SiLU uses the hardware tanh approximation (relative error
+    # about 2^-11) and its FP32 sums run in another order than PyTorch's, so
+    # an activation near a bf16 rounding boundary can round the other way
+    # (one bf16 ulp, 2^-8 relative) and move that prediction.
+    assert float(diff.max()) <= 1e-2 * scale, (float(diff.max()), scale)
+    assert q999 <= 2e-3 * scale, (q999, scale)
+    assert float(diff.mean()) <= 2e-4 * scale
     # and close to the fp32 network
     f32 = _torch_forward(net, s, shapes)
     assert float((d - f32).abs().max()) <= 3e-2 * scale
