@@ -53,6 +53,7 @@ _SIGS = {
     "fcdemSetCollidePath": (None, [C.c_int]),
     "fcdemSetCellCulling": (None, [C.c_int]),
     "fcdemSetCrowdPath": (None, [C.c_int]),
+    "fcdemSetCellOrder": (None, [C.c_int]),
     "fcdemSetCrowdLimit": (None, [C.c_uint]),
     "fcdemSetUpdatePipeline": (None, [C.c_int]),
     "fcdemAutotuneSort": (C.c_int, [C.c_uint, C.c_uint, C.POINTER(C.c_float)]),

@@ -147,6 +147,7 @@ fcdemBatch *fcdemBatchCreate(const fcdemBatchScene *scenes, uint numScenes, int 
     std::memset(&d, 0, sizeof(d));
     d.p = p;
     d.p.numCells = (unsigned)cells;
+    d.p.maxParticlesPerCell = 0u;  // linear cell keys in a batch
     for (int k = 0; k < 3; ++k) {
       d.lo[k] = in.boxLo[k];
       d.hi[k] = in.boxHi[k];

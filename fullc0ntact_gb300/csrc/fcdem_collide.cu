@@ -239,7 +239,7 @@ __device__ __forceinline__ float3 neighbourForceGlobal(
     if (rowD2 > cullR2) continue;
     const bool useL = rowD2 + CellCull::pick(-1, cc.xl, cc.xh) <= cullR2;
     const bool useR = rowD2 + CellCull::pick(1, cc.xl, cc.xh) <= cullR2;
-    if (kPrefix) {
+    if (kPrefix && !mortonOrder(P)) {
       const unsigned gxm = P.gridSize[0] - 1u;
       const unsigned xm = (unsigned)(g.x) & gxm;
       if (xm >= 1u && xm < gxm) {
@@ -341,7 +341,7 @@ __device__ __forceinline__ unsigned neighbourhoodCount(int3 g, const CellRanges 
   unsigned total = 0;
   const unsigned gxm = P.gridSize[0] - 1u;
   const unsigned xm = (unsigned)(g.x) & gxm;
-  if (kPrefix && xm >= 1u && xm < gxm) {
+  if (kPrefix && xm >= 1u && xm < gxm && !mortonOrder(P)) {
     // no x wrap: each row's three cells are consecutive hashes
 #pragma unroll
     for (int row = 0; row < 9; row++) {
@@ -871,7 +871,9 @@ void launchCollide(int mode, bool collider, float4 *newVel, const float4 *sp,
   const bool prefix = cells.off != nullptr;
   // The bulk copies need 16-byte aligned positions; the tiled kernel is
   // opt-in (fcdemSetCollidePath(1)): the culled global kernel is faster.
-  bool tiled = !prefix && g_collidePath == 1 && ((uintptr_t)sp & 15u) == 0;
+  // (its row windows assume the linear cell order)
+  bool tiled = !prefix && g_collidePath == 1 && ((uintptr_t)sp & 15u) == 0 &&
+               kp.p.maxParticlesPerCell != kMortonTag;
   // Culling is exact when every grid dimension is >= 3 and the largest
   // contact distance 2 * particleRadius fits in the smallest cell.
   const SimParams &P = kp.p;

@@ -126,9 +126,15 @@ void *scratch(Context &c, size_t bytes) {
   return c.scratch;
 }
 
+bool mortonUsable(const SimParams &p) {
+  return p.gridSize[0] == p.gridSize[1] && p.gridSize[1] == p.gridSize[2] &&
+         p.gridSize[0] >= 1u && p.gridSize[0] <= 1024u;
+}
+
 KParams kparams(const Context &c) {
   KParams k;
   k.p = c.params;
+  k.p.maxParticlesPerCell = (c.morton && mortonUsable(c.params)) ? kMortonTag : 0u;
   k.radiusFromW = c.radiusFromW;
   return k;
 }
@@ -258,6 +264,8 @@ const char *fcdemGetErrorString(int code) {
 void fcdemSetStream(void *stream) { t_stream = (cudaStream_t)stream; }
 
 void fcdemSetRadiusMode(int radiusFromW) { ctx().radiusFromW = radiusFromW ? 1 : 0; }
+
+void fcdemSetCellOrder(int morton) { ctx().morton = morton ? 1 : 0; }
 
 const char *fcdemVersion(void) { return "fcdem-gb300 0.1 (sm_103a)"; }
 

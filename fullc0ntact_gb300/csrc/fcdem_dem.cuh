@@ -23,13 +23,35 @@ __device__ __forceinline__ int3 gridPos(float px, float py, float pz,
   return g;
 }
 
+// Cell-key order.  The library's own copy of SimParams carries kMortonTag in
+// maxParticlesPerCell (a field the reference never reads) when
+// fcdemSetCellOrder(1) is on and the grid is cubic: every cell key is then
+// the Morton code of the wrapped cell coordinates instead of the linear
+// hash.  Morton order keeps cells that are near in space near in the sorted
+// arrays; the per-cell contents and their order are the same either way.
+// Bits 0..9 of v moved to bits 0, 3, 6, ... 27 (3-D Morton spread).
+__device__ __forceinline__ unsigned mortonSpread(unsigned v) {
+  v &= 0x3ffu;
+  v = (v | (v << 16)) & 0x030000ffu;
+  v = (v | (v << 8)) & 0x0300f00fu;
+  v = (v | (v << 4)) & 0x030c30c3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+
+__device__ __forceinline__ bool mortonOrder(const SimParams &P) {
+  return P.maxParticlesPerCell == kMortonTag;
+}
+
 // particles_kernel.cu:88-94 (calcGridHash): power-of-two wrap, 24-bit
-// multiplies.
+// multiplies -- or, in Morton order, the interleaved bits of the wrapped
+// coordinates (x lowest).
 __device__ __forceinline__ unsigned gridHash(int gx, int gy, int gz,
                                              const SimParams &P) {
   unsigned x = (unsigned)gx & (P.gridSize[0] - 1u);
   unsigned y = (unsigned)gy & (P.gridSize[1] - 1u);
   unsigned z = (unsigned)gz & (P.gridSize[2] - 1u);
+  if (mortonOrder(P)) return mortonSpread(x) | (mortonSpread(y) << 1) | (mortonSpread(z) << 2);
   return __umul24(__umul24(z, P.gridSize[1]), P.gridSize[0]) +
          __umul24(y, P.gridSize[0]) + x;
 }

@@ -48,6 +48,7 @@ struct Context {
   bool haveParams = false;
   SimParams params{};
   int radiusFromW = 0;
+  int morton = 0;               // fcdemSetCellOrder
   unsigned *dStatus = nullptr;  // one device word of kStatus* bits
   void *scratch = nullptr;      // grown on demand, never shrunk
   size_t scratchBytes = 0;
@@ -82,6 +83,11 @@ void stageEnd(int stage);
 void *scratch(Context &c, size_t bytes);
 
 KParams kparams(const Context &c);
+// Morton cell keys need a cubic power-of-two grid of at most 1024 cells a side.
+// The library's parameter copy marks Morton order with this value in
+// maxParticlesPerCell (unused by the reference); see gridHash.
+constexpr unsigned kMortonTag = 0x4d4f5254u;
+bool mortonUsable(const SimParams &p);
 
 // Number of key bits a sort must cover for keys below numCells.
 inline int keyBits(unsigned numCells) {

@@ -189,6 +189,18 @@ void fcdemSetCrowdPath(int on);
  * (0: the default, 1024). */
 void fcdemSetCrowdLimit(uint limit);
 
+/* Cell-key order (no counterpart in the reference; default 0, the
+ * reference's linear hash z*gy*gx + y*gx + x).  1: Morton order -- the cell
+ * key of every stage (calcHash, the sort, the cell tables, collide,
+ * fcdemUpdate, fcdemUM_update) is the 3-D Morton code of the wrapped cell
+ * coordinates, so cells near in space are near in the sorted arrays.
+ * Needs a cubic power-of-two grid of at most 1024 cells a side (other grids
+ * keep the linear order).  The members of each cell and their order are the
+ * same as in linear order, so positions, velocities and forces are
+ * identical; hash[] and the cellStart/cellEnd tables are indexed by the
+ * Morton key instead. */
+void fcdemSetCellOrder(int morton);
+
 /* Library version string. */
 const char *fcdemVersion(void);
 
