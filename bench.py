@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the batched-scenes measurement")
+    ap.add_argument("--cell-order", choices=["linear", "morton"], default="linear",
+                    help="cell keys of the headline job (results are identical)")
     ap.add_argument("--no-config2", action="store_true",
                     help="skip the torus-obstacle (distance map / neural SDF) measurement")
     ap.add_argument("--config2-n", type=int, default=1048576)
@@ -557,6 +559,7 @@ def run_ours(args):
 
     sc = load_scene(args.n)
     n = sc["pos"].shape[0]
+    lib.fcdemSetCellOrder(1 if args.cell_order == "morton" else 0)
     ds = dem.DeviceScene(sc, f"cuda:{dev}")
     # project autotuner: the sort's block shape for this size (setup, untimed)
     tuned_ms = C.c_float()
@@ -662,6 +665,7 @@ def run_ours(args):
     e2e = replica_throughput(n, e2e_steps, e2e_s, world)
     clk = clocks.stop()
 
+    lib.fcdemSetCellOrder(0)
     config2 = None
     if not args.no_config2:
         config2 = measure_config2(args.config2_n, args.config2_steps, dev)
@@ -691,7 +695,7 @@ def run_ours(args):
             "config": {"workload": f"{WORKLOAD}, {args.steps}-step job from the packed state",
                        "n": n, "grid": 256, "cells": ncell,
                        "occupied_cells": occupied, "step": "fcdemUpdate (fused update)",
-                       "sort_config": sort_cfg,
+                       "sort_config": sort_cfg, "cell_order": args.cell_order,
                        "l2": "inputs larger than L2 (no flush)",
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
