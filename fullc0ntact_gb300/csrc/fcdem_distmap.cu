@@ -2,7 +2,9 @@
 // cuda_addon/distancemap.cuh:118-302, cuda_addon/boundaries.cuh:38-89) and
 // the particledem_um entry points that use it (cuda_addon/particledem_um.cu).
 // The map types and the query live in fcdem_map.cuh.
+#include <algorithm>
 #include <cmath>
+#include <vector>
 #include <cstdlib>
 
 #include "fcdem_map.cuh"
@@ -126,6 +128,106 @@ kRoundedBoxMap(float4 *__restrict__ vert, int vx, int vy, int vz, float3 vmin, f
     }
     vert[t] = make_float4((float)d, (float)cp[0], (float)cp[1], (float)cp[2]);
   }
+}
+
+// Closest point of triangle (a, b, c) to p: the region-based method of
+// Ericson, Real-Time Collision Detection, section 5.1.5 (vertex, edge or face
+// region from the barycentric signs).
+__device__ __forceinline__ float3 closestOnTriangle(float3 p, float3 a, float3 b, float3 c) {
+  const float3 ab = make_float3(b.x - a.x, b.y - a.y, b.z - a.z);
+  const float3 ac = make_float3(c.x - a.x, c.y - a.y, c.z - a.z);
+  const float3 ap = make_float3(p.x - a.x, p.y - a.y, p.z - a.z);
+  auto dot = [](float3 u, float3 v) { return u.x * v.x + u.y * v.y + u.z * v.z; };
+  auto lerp = [](float3 o, float3 d, float t) {
+    return make_float3(o.x + t * d.x, o.y + t * d.y, o.z + t * d.z);
+  };
+  const float d1 = dot(ab, ap), d2 = dot(ac, ap);
+  if (d1 <= 0.0f && d2 <= 0.0f) return a;
+  const float3 bp = make_float3(p.x - b.x, p.y - b.y, p.z - b.z);
+  const float d3 = dot(ab, bp), d4 = dot(ac, bp);
+  if (d3 >= 0.0f && d4 <= d3) return b;
+  const float vc = d1 * d4 - d3 * d2;
+  if (vc <= 0.0f && d1 >= 0.0f && d3 <= 0.0f) return lerp(a, ab, d1 / (d1 - d3));
+  const float3 cp = make_float3(p.x - c.x, p.y - c.y, p.z - c.z);
+  const float d5 = dot(ab, cp), d6 = dot(ac, cp);
+  if (d6 >= 0.0f && d5 <= d6) return c;
+  const float vb = d5 * d2 - d1 * d6;
+  if (vb <= 0.0f && d2 >= 0.0f && d6 <= 0.0f) return lerp(a, ac, d2 / (d2 - d6));
+  const float va = d3 * d6 - d5 * d4;
+  if (va <= 0.0f && (d4 - d3) >= 0.0f && (d5 - d6) >= 0.0f) {
+    const float3 bc = make_float3(c.x - b.x, c.y - b.y, c.z - b.z);
+    return lerp(b, bc, (d4 - d3) / ((d4 - d3) + (d5 - d6)));
+  }
+  const float den = 1.0f / (va + vb + vc);
+  const float v = vb * den, w = vc * den;
+  return make_float3(a.x + ab.x * v + ac.x * w, a.y + ab.y * v + ac.y * w,
+                     a.z + ab.z * v + ac.z * w);
+}
+
+// Solid angle of triangle (a, b, c) seen from p, signed by the triangle's
+// orientation (Van Oosterom and Strackee, IEEE Trans. Biomed. Eng. 30, 1983).
+__device__ __forceinline__ float solidAngle(float3 p, float3 a, float3 b, float3 c) {
+  const float3 A = make_float3(a.x - p.x, a.y - p.y, a.z - p.z);
+  const float3 B = make_float3(b.x - p.x, b.y - p.y, b.z - p.z);
+  const float3 C = make_float3(c.x - p.x, c.y - p.y, c.z - p.z);
+  const float la = sqrtf(A.x * A.x + A.y * A.y + A.z * A.z);
+  const float lb = sqrtf(B.x * B.x + B.y * B.y + B.z * B.z);
+  const float lc = sqrtf(C.x * C.x + C.y * C.y + C.z * C.z);
+  const float det = A.x * (B.y * C.z - B.z * C.y) - A.y * (B.x * C.z - B.z * C.x) +
+                    A.z * (B.x * C.y - B.y * C.x);
+  const float den = la * lb * lc + (A.x * B.x + A.y * B.y + A.z * B.z) * lc +
+                    (A.x * C.x + A.y * C.y + A.z * C.z) * lb +
+                    (B.x * C.x + B.y * C.y + B.z * C.z) * la;
+  return 2.0f * atan2f(det, den);
+}
+
+constexpr int kMeshChunk = 256;
+
+// Distance map of a closed, outward-oriented triangle mesh: at every lattice
+// vertex the distance to the closest point of the mesh, negative inside (the
+// generalized winding number, the summed solid angles over 4 pi, above 1/2),
+// and that closest point as the contact point -- what DistanceMapMesh::
+// ComputeDistance (distancegridcgal.hpp:36-69) stores.  One thread per
+// vertex; the triangles go through shared memory in chunks.
+__global__ void __launch_bounds__(128)
+kMeshMap(float4 *__restrict__ vert, int vx, int vy, int vz, float3 vmin, float cs,
+         const float4 *__restrict__ tri, unsigned nt) {
+  __shared__ float4 sTri[kMeshChunk * 3];
+  const long long total = (long long)vx * vy * vz;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = t < total;
+  float3 p = make_float3(0.0f, 0.0f, 0.0f);
+  if (valid) {
+    const int i = (int)(t % vx), j = (int)((t / vx) % vy), k = (int)(t / ((long long)vx * vy));
+    p = make_float3(vcoord(vmin.x, i, cs), vcoord(vmin.y, j, cs), vcoord(vmin.z, k, cs));
+  }
+  float best = 3.4e38f;
+  float3 bestCp = p;
+  float omega = 0.0f;
+  for (unsigned base = 0; base < nt; base += kMeshChunk) {
+    const unsigned cnt = min((unsigned)kMeshChunk, nt - base);
+    __syncthreads();
+    for (unsigned e = threadIdx.x; e < cnt * 3; e += blockDim.x) sTri[e] = __ldg(tri + base * 3 + e);
+    __syncthreads();
+    if (!valid) continue;
+    for (unsigned q = 0; q < cnt; ++q) {
+      const float4 a4 = sTri[3 * q], b4 = sTri[3 * q + 1], c4 = sTri[3 * q + 2];
+      const float3 a = make_float3(a4.x, a4.y, a4.z), b = make_float3(b4.x, b4.y, b4.z),
+                   c = make_float3(c4.x, c4.y, c4.z);
+      const float3 cp = closestOnTriangle(p, a, b, c);
+      const float dx = p.x - cp.x, dy = p.y - cp.y, dz = p.z - cp.z;
+      const float d2 = dx * dx + dy * dy + dz * dz;
+      if (d2 < best) {
+        best = d2;
+        bestCp = cp;
+      }
+      omega += solidAngle(p, a, b, c);
+    }
+  }
+  if (!valid) return;
+  const bool inside = omega > 2.0f * 3.14159265358979f;  // winding number > 1/2
+  const float d = sqrtf(best);
+  vert[t] = make_float4(inside ? -d : d, bestCp.x, bestCp.y, bestCp.z);
 }
 
 }  // namespace
@@ -257,6 +359,69 @@ fcdemDistanceMap *fcdemDistMapRoundedBox(const float halfExtents[3], float round
       make_float3(vmin[0], vmin[1], vmin[2]), cs,
       make_float3(halfExtents[0], halfExtents[1], halfExtents[2]), rounding);
   launchOk();
+  return m;
+}
+
+fcdemDistanceMap *fcdemDistMapFromMesh(const float *vertices3, uint numVertices,
+                                       const uint *triangles3, uint numTriangles,
+                                       int cellsPerAxis, float margin) {
+  if (!vertices3 || !triangles3 || numVertices < 3 || numTriangles < 1 || cellsPerAxis < 1 ||
+      !(margin >= 0.0f)) {
+    setError(FCDEM_ERR_INVALID_VALUE);
+    return nullptr;
+  }
+  float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+  for (uint v = 0; v < numVertices; ++v)
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = std::fmin(lo[a], vertices3[3 * v + a]);
+      hi[a] = std::fmax(hi[a], vertices3[3 * v + a]);
+    }
+  std::vector<float4> tri((size_t)numTriangles * 3);
+  for (uint t = 0; t < numTriangles; ++t)
+    for (int c = 0; c < 3; ++c) {
+      const uint v = triangles3[3 * t + c];
+      if (v >= numVertices) { setError(FCDEM_ERR_INVALID_VALUE); return nullptr; }
+      tri[3 * t + c] = make_float4(vertices3[3 * v], vertices3[3 * v + 1], vertices3[3 * v + 2], 0.0f);
+    }
+  // cubic cells over the mesh box plus the margin, centred on the box: the
+  // largest axis cut into cellsPerAxis cells, the others into whole cells
+  float centre[3], ex[3], big = 0.0f;
+  for (int a = 0; a < 3; ++a) {
+    centre[a] = 0.5f * (lo[a] + hi[a]);
+    ex[a] = 0.5f * (hi[a] - lo[a]) + margin;
+    big = std::fmax(big, ex[a]);
+  }
+  if (!(big > 0.0f)) { setError(FCDEM_ERR_INVALID_VALUE); return nullptr; }
+  const float cs = 2.0f * big / (float)cellsPerAxis;
+  int cells[3];
+  float vmin[3], vmax[3];
+  for (int a = 0; a < 3; ++a) {
+    cells[a] = std::max(1, (int)std::ceil(2.0f * ex[a] / cs));
+    vmin[a] = centre[a] - 0.5f * cells[a] * cs;
+    vmax[a] = vmin[a] + cells[a] * cs;
+  }
+  fcdemDistanceMap *m = fcdemDistMapCreate(nullptr, nullptr, vmin, vmax, cs, cells);
+  if (!m) return nullptr;
+  float4 *dTri = nullptr;
+  if (cudaMalloc(&dTri, tri.size() * sizeof(float4)) != cudaSuccess) {
+    cudaGetLastError();
+    fcdemDistMapDestroy(m);
+    setError(FCDEM_ERR_ALLOC);
+    return nullptr;
+  }
+  bool ok = cudaOk(cudaMemcpy(dTri, tri.data(), tri.size() * sizeof(float4), cudaMemcpyHostToDevice));
+  const long long total = (long long)(cells[0] + 1) * (cells[1] + 1) * (cells[2] + 1);
+  if (ok) {
+    kMeshMap<<<(unsigned)((total + 127) / 128), 128, 0, curStream()>>>(
+        m->vert, cells[0] + 1, cells[1] + 1, cells[2] + 1, make_float3(vmin[0], vmin[1], vmin[2]),
+        cs, dTri, numTriangles);
+    ok = launchOk() && cudaOk(cudaStreamSynchronize(curStream()));
+  }
+  cudaFree(dTri);
+  if (!ok) {
+    fcdemDistMapDestroy(m);
+    return nullptr;
+  }
   return m;
 }
 

@@ -212,6 +212,8 @@ _DM_SIGS = {
                                         C.POINTER(C.c_float), C.c_float, C.POINTER(C.c_int)]),
     "fcdemDistMapTorus": (C.c_void_p, [C.c_float, C.c_float, C.c_int, C.c_float]),
     "fcdemDistMapDestroy": (None, [C.c_void_p]),
+    "fcdemDistMapFromMesh": (C.c_void_p, [C.c_void_p, C.c_uint, C.c_void_p, C.c_uint, C.c_int,
+                                          C.c_float]),
     "fcdemDistMapGeometry": (None, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                     C.POINTER(C.c_float), C.POINTER(C.c_int)]),
     "fcdemDistMapVertices": (None, [C.c_void_p, C.c_void_p]),
@@ -257,6 +259,17 @@ class DistanceMap:
     def rounded_box(cls, half_extents, rounding=0.02, cells_per_axis=128, margin=0.05):
         h = lib.fcdemDistMapRoundedBox(_f3(half_extents), rounding, cells_per_axis, margin)
         check("fcdemDistMapRoundedBox")
+        return cls(h)
+
+    @classmethod
+    def from_mesh(cls, vertices, triangles, cells_per_axis=128, margin=0.05):
+        """Map of a closed, outward-oriented triangle mesh computed on the GPU
+        (vertices (nv, 3) float, triangles (nt, 3) vertex indices)."""
+        v = np.ascontiguousarray(vertices, np.float32)
+        t = np.ascontiguousarray(triangles, np.uint32)
+        h = lib.fcdemDistMapFromMesh(v.ctypes.data, v.shape[0], t.ctypes.data, t.shape[0],
+                                     cells_per_axis, margin)
+        check("fcdemDistMapFromMesh")
         return cls(h)
 
     @classmethod

@@ -245,3 +245,26 @@ def batch_config4(num_scenes: int = 128, n_min: int = 4096, n_max: int = 262144,
     shape = [k % num_shapes for k in range(num_scenes)]
     scs = [obstacle_scene(int(n), obs[shape[k]], seed * 100003 + k) for k, n in enumerate(sizes)]
     return scs, obs, shape
+
+
+def torus_mesh(major_radius: float = 0.3, tube_radius: float = 0.1, nu: int = 256,
+               nv: int = 64):
+    """The procedural torus obstacle as a closed triangle mesh: nu x nv quads
+    of the (u around z, v around the tube) parametrisation
+    ((R + r cos v) cos u, (R + r cos v) sin u, r sin v), each split into two
+    triangles ordered so that their normals point outwards.  Returns
+    (vertices (nu*nv, 3) float32, triangles (2*nu*nv, 3) uint32)."""
+    u = 2.0 * np.pi * np.arange(nu) / nu
+    v = 2.0 * np.pi * np.arange(nv) / nv
+    U, V = np.meshgrid(u, v, indexing="ij")
+    rho = major_radius + tube_radius * np.cos(V)
+    verts = np.stack([rho * np.cos(U), rho * np.sin(U), tube_radius * np.sin(V)], -1)
+    verts = verts.reshape(-1, 3).astype(np.float32)
+    i, j = np.meshgrid(np.arange(nu), np.arange(nv), indexing="ij")
+    a = i * nv + j
+    b = ((i + 1) % nu) * nv + j
+    c = ((i + 1) % nu) * nv + (j + 1) % nv
+    d = i * nv + (j + 1) % nv
+    tris = np.concatenate([np.stack([a, b, c], -1).reshape(-1, 3),
+                           np.stack([a, c, d], -1).reshape(-1, 3)]).astype(np.uint32)
+    return verts, tris

@@ -275,6 +275,16 @@ fcdemDistanceMap *fcdemDistMapTorus(float majorRadius, float tubeRadius, int cel
  * signed distance and closest point at every vertex. */
 fcdemDistanceMap *fcdemDistMapRoundedBox(const float halfExtents[3], float rounding,
                                          int cellsPerAxis, float margin);
+/* A map of a closed, outward-oriented triangle mesh (host arrays: xyz per
+ * vertex, three vertex indices per triangle), computed on the GPU: at every
+ * vertex the distance to the closest point of the mesh, negative inside (by
+ * the generalized winding number), and that closest point as the contact
+ * point -- what the reference's CGAL builder stores
+ * (distancegridcgal.hpp:36-69).  Cubic cells over the mesh box plus the
+ * margin, the largest axis cut into cellsPerAxis cells.  Synchronises. */
+fcdemDistanceMap *fcdemDistMapFromMesh(const float *vertices3, uint numVertices,
+                                       const uint *triangles3, uint numTriangles,
+                                       int cellsPerAxis, float margin);
 void fcdemDistMapDestroy(fcdemDistanceMap *map);
 void fcdemDistMapGeometry(const fcdemDistanceMap *map, float vmin[3], float vmax[3],
                           float *cellSize, int cells[3]);
