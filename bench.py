@@ -270,7 +270,11 @@ def measure_config2(n: int, steps: int, dev: int) -> dict:
     import torch
     from fullc0ntact_gb300 import dem, scenes, sdf
     lib = dem.lib
-    dmap = dem.DistanceMap.torus(0.3, 0.1, 128, 0.05)
+    # the obstacle: the 256 x 64-quad torus mesh, its 128-cell map built on the GPU
+    t_map = time.perf_counter()
+    verts, tris = scenes.torus_mesh(0.3, 0.1, 256, 64)
+    dmap = dem.DistanceMap.from_mesh(verts, tris, 128, 0.05)
+    map_s = time.perf_counter() - t_map
     net = sdf.SdfNet(3, 64, 3, seed=5)
     net.normalize_to(dmap)
     train = sdf.samples(dmap, 2_000_000, 0.6, 0.05, seed=21)
@@ -347,9 +351,11 @@ def measure_config2(n: int, steps: int, dev: int) -> dict:
         del us
     same = all(torch.equal(a.view(torch.int32), b.view(torch.int32))
                for a, b in zip(finals["plain"], finals["neural"]))
-    return {"workload": f"{n} spheres r=1/256 falling onto a torus (R 0.3, r 0.1), 128^3 "
-                        "distance map, unified-memory step (calcHash, sort, reorder, "
+    return {"workload": f"{n} spheres r=1/256 falling onto a torus (R 0.3, r 0.1; mesh of "
+                        "256 x 64 quads, 32768 triangles), 128-cell distance map built from the "
+                        "mesh on the GPU, unified-memory step (calcHash, sort, reorder, "
                         f"evalForces, integrate with map/cylinder/planes), {steps} steps",
+            "map_build_s": map_s,
             "n": n, "steps": steps, "unit": UNIT,
             "plain_exact_map": out["plain"], "neural_sdf": out["neural"],
             "speedup": out["neural"]["value"] / out["plain"]["value"],
