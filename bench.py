@@ -647,6 +647,17 @@ def run_ours(args):
     peak, peak_kind = measured_peak_gbs()
     achieved = algo[dominant] / (stage_ms[dominant] / 1e3) / 1e9
     traffic = profile_traffic(f"fcdem_{dominant}", n)
+    # per stage of the counting pipeline: stage 1 is the reference's sort and
+    # reorder together (scan 8 C, scatter + fix-up gather 88 N); stage 2 the
+    # cell tables written once per call
+    stage_bytes = {"integrate_hash": 72 * n, "sort": 88 * n + 8 * ncell, "fill": 8 * ncell,
+                   "collide": 72 * n + 8 * occupied}
+    stage_roofline = {}
+    for k, b in stage_bytes.items():
+        if stage_ms.get(k):
+            gbs = b / (stage_ms[k] / 1e3) / 1e9
+            stage_roofline[k] = {"algorithmic_bytes": b, "ms": stage_ms[k], "achieved_gbs": gbs,
+                                 "frac": gbs / peak}
 
     # --- end to end through the C-ABI with host buffers --------------------
     hpos = torch.empty((n, 4), dtype=torch.float32).pin_memory()
@@ -714,6 +725,7 @@ def run_ours(args):
                          "traffic": traffic, "algorithmic_bytes": algo[dominant],
                          "avg_launch_ms": stage_ms[dominant]},
             "stage_ms": stage_ms,
+            "stage_roofline": stage_roofline,
             "phases": phases,
             "final_cells": final_cells,
             "batched": batched,
