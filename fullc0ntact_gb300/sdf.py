@@ -184,13 +184,14 @@ def shape_net(maps: list, samples_per_map: int = 500_000, hidden: int = 128, lay
     return net, loss
 
 
-def calibrate_skin(net: SdfNet, maps: list, radius: float, samples_per_map: int = 200_000,
-                   seed: int = 300, shaped: bool = True) -> tuple:
+def calibrate_skin(net: SdfNet, maps: list, radius: float, samples_per_map: int = 500_000,
+                   seed: int = 300, shaped: bool = True, margin: float = 0.5) -> tuple:
     """The culling threshold, judged by the exact maps: on held-out samples
     of every map, p_max = the largest prediction at a point the map puts
     within one radius of the surface (or inside the obstacle), the value that
-    must not be culled.  The skin is max(2 radius, p_max + 0.25 (p_max -
-    radius)).  Returns (skin, p_max)."""
+    must not be culled.  The skin is max(2 radius, p_max + margin (p_max -
+    radius)); the margin covers points the samples missed.  Returns
+    (skin, p_max)."""
     p_max = -1e30
     for k, m in enumerate(maps):
         if shaped:
@@ -201,4 +202,4 @@ def calibrate_skin(net: SdfNet, maps: list, radius: float, samples_per_map: int 
         touching = val[:, 3] < radius
         if bool(touching.any()):
             p_max = max(p_max, float(pred[touching].max()))
-    return max(2.0 * radius, p_max + 0.25 * max(p_max - radius, 0.0)), p_max
+    return max(2.0 * radius, p_max + margin * max(p_max - radius, 0.0)), p_max
