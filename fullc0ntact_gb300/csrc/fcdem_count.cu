@@ -88,6 +88,65 @@ kScanTiles(unsigned *__restrict__ tileCnt, unsigned *__restrict__ tileOff, unsig
   if (tid == 0) tileOff[tiles] = sCarry;
 }
 
+// The same prefix over many tiles (batches of many scenes: tens of
+// thousands of tiles), in two short launches instead of one CTA walking them
+// all: kScanTileBlocks scans each block of 1024 tile counts and writes its
+// total, kAddTileBlocks adds the totals of the blocks before.
+constexpr unsigned kTileBlock = 1024;
+constexpr unsigned kTilesOneCta = 8192;  // up to this many tiles kScanTiles runs alone
+
+__global__ void __launch_bounds__(kTileBlock)
+kScanTileBlocks(unsigned *__restrict__ tileCnt, unsigned *__restrict__ tileOff, unsigned tiles,
+                unsigned *__restrict__ blockSum, unsigned *__restrict__ largeCount) {
+  __shared__ unsigned sWarp[32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (blockIdx.x == 0 && tid == 0) *largeCount = 0u;
+  const unsigned t = blockIdx.x * kTileBlock + tid;
+  const unsigned v = t < tiles ? tileCnt[t] : 0u;
+  unsigned x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sWarp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    unsigned w = sWarp[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    sWarp[lane] = w;
+  }
+  __syncthreads();
+  if (t < tiles) {
+    tileOff[t] = (warp ? sWarp[warp - 1] : 0u) + x - v;
+    tileCnt[t] = 0u;
+  }
+  if (tid == 0) blockSum[blockIdx.x] = sWarp[31];
+}
+
+__global__ void __launch_bounds__(kTileBlock)
+kAddTileBlocks(unsigned *__restrict__ tileOff, unsigned tiles,
+               const unsigned *__restrict__ blockSum) {
+  __shared__ unsigned sPart[32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  unsigned part = 0;
+  for (unsigned b = tid; b < blockIdx.x; b += kTileBlock) part += __ldg(blockSum + b);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+  if (lane == 0) sPart[warp] = part;
+  __syncthreads();
+  unsigned carry = 0;
+  for (int w = 0; w < (int)(kTileBlock / 32); ++w) carry += sPart[w];
+  const unsigned t = blockIdx.x * kTileBlock + tid;
+  if (t < tiles) tileOff[t] += carry;
+  if (blockIdx.x == gridDim.x - 1 && tid == 0)
+    tileOff[tiles] = carry + __ldg(blockSum + blockIdx.x);
+}
+
 // off[c] = tileOff[tile] + exclusive prefix of cnt within the tile, cnt
 // cleared.  A tile without particles only writes its constant offsets.
 // Round q of a tile covers cells q*1024 .. +1024, thread t the four at 4t
@@ -476,8 +535,9 @@ bool countBuffersIn(void *&buf, size_t &bytes, unsigned &cells, unsigned n, unsi
   const unsigned tiles = (unsigned)((m + kScanTile - 1) / kScanTile);
   auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
   const unsigned largeCap = largeCapacity(n);
+  const unsigned tileBlocks = (tiles + kTileBlock - 1) / kTileBlock;
   const size_t need = 2 * al(m * 4) + 4 * al((size_t)n * 4) + 2 * al((size_t)(tiles + 1) * 4) +
-                      al(((size_t)largeCap + 1) * 4);
+                      al(((size_t)largeCap + 1) * 4) + al((size_t)tileBlocks * 4);
   if (buf == nullptr || bytes < need || cells != numCells) {
     if (!cudaOk(cudaDeviceSynchronize())) return false;
     if (buf) cudaFree(buf);
@@ -515,6 +575,8 @@ bool countBuffersIn(void *&buf, size_t &bytes, unsigned &cells, unsigned n, unsi
   p += al((size_t)n * 4);
   b.large = (unsigned *)p;
   b.largeCap = largeCap;
+  p += al(((size_t)largeCap + 1) * 4);
+  b.tileBlockSum = (unsigned *)p;
   b.scanTiles = tiles;
   return true;
 }
@@ -552,8 +614,17 @@ bool countPipelineSort(Context &c, const CountBuffers &b, const unsigned *origOf
                        unsigned numCells) {
   cudaStream_t st = curStream();
   const unsigned m = numCells + 1;
-  kScanTiles<<<1, 1024, 0, st>>>(b.tileCnt, b.tileOff, b.scanTiles, b.large);
-  if (!launchOk()) return false;
+  if (b.scanTiles <= kTilesOneCta) {
+    kScanTiles<<<1, 1024, 0, st>>>(b.tileCnt, b.tileOff, b.scanTiles, b.large);
+    if (!launchOk()) return false;
+  } else {
+    const unsigned blocks = (b.scanTiles + kTileBlock - 1) / kTileBlock;
+    kScanTileBlocks<<<blocks, kTileBlock, 0, st>>>(b.tileCnt, b.tileOff, b.scanTiles,
+                                                   b.tileBlockSum, b.large);
+    if (!launchOk()) return false;
+    kAddTileBlocks<<<blocks, kTileBlock, 0, st>>>(b.tileOff, b.scanTiles, b.tileBlockSum);
+    if (!launchOk()) return false;
+  }
   kScanCells<<<b.scanTiles, kScanThreads, 0, st>>>(b.cnt, b.off, m, b.tileOff);
   if (!launchOk()) return false;
   // hash holds the new hashes in entry order until the fix-up overwrites it

@@ -162,6 +162,7 @@ struct CountBuffers {
   unsigned *cnt, *off, *rank, *slotKey, *slotIdx, *slotPrev;
   unsigned *tileCnt, *tileOff;  // per 4096-cell tile: counts and their prefix
   unsigned *large;              // [0] = count, [1..largeCap] = cells too full for the re-rank
+  unsigned *tileBlockSum;       // per 1024 tiles: their total (many-tile scans)
   unsigned scanTiles, largeCap;
 };
 bool countPipelineBegin(Context &c, float4 *pos, float4 *vel, float dt, unsigned *hash,
