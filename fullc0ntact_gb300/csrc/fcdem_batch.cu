@@ -71,7 +71,7 @@ bool runBatchObstacles(fcdemBatch *b, const CountBuffers &cb, float4 *pos, float
   Context &c = ctx();
   const UmCount count{b->hash, cb.rank, cb.cnt, cb.tileCnt};
   if (!batchObstacleIntegrate(b->scenes, b->sceneOf, b->radiusFromW, b->maps, b->net, b->skin,
-                              pos, pos, vel, dt, b->n, &count, b->exact))
+                              pos, pos, vel, dt, b->n, &count, b->exact, 0))
     return false;
   for (unsigned s = 0; s < steps; ++s) {
     if (!countPipelineSort(c, cb, s == 0 ? nullptr : b->index, pos, vel, b->hash, b->index,
@@ -84,7 +84,7 @@ bool runBatchObstacles(fcdemBatch *b, const CountBuffers &cb, float4 *pos, float
                        b->sortedVel, b->index, cb.off, b->n, out);
     if (!last &&
         !batchObstacleIntegrate(b->scenes, b->sceneOf, b->radiusFromW, b->maps, b->net, b->skin,
-                                b->sortedPos, pos, vel, dt, b->n, &count, b->exact))
+                                b->sortedPos, pos, vel, dt, b->n, &count, b->exact, s + 1))
       return false;
   }
   return true;
@@ -231,6 +231,7 @@ void fcdemBatchSetObstacles(fcdemBatch *b, const fcdemDistanceMap *const *maps, 
   b->net = numMaps ? net : nullptr;
   b->skin = skin;
   if (numMaps == 0) return;
+  if (net) sdfHints(net, (b->n + 127) / 128);  // now, not while a graph is recorded
   std::vector<MapView> hv(numMaps);
   for (uint k = 0; k < numMaps; ++k) hv[k] = view(maps[k]);
   if (cudaMalloc(&b->maps, sizeof(MapView) * numMaps) != cudaSuccess ||

@@ -206,10 +206,15 @@ struct MapView;
 bool batchObstacleIntegrate(const BatchScene *scenes, const unsigned *sceneOf, bool radiusFromW,
                             const MapView *maps, fcdemSdfNet *net, float skin,
                             const float4 *inPos, float4 *pos, float4 *vel, float dt,
-                            unsigned n, const UmCount *count, unsigned *exact);
+                            unsigned n, const UmCount *count, unsigned *exact, unsigned step);
 // The same with the neural-SDF culling of the map query (fcdem_sdf.cu).
+// The network's per-tile culling hints for `tiles` tiles, allocated (and
+// cleared) when they grow; nullptr when they cannot be had.
+unsigned char *sdfHints(fcdemSdfNet *net, unsigned tiles);
+// `step` (the step's number within a call) chooses the refresh steps of the
+// per-tile culling hints; -1: a lone call, no hints.
 bool sdfIntegrate(fcdemSdfNet *net, float4 *pos, float4 *vel, float dt, unsigned n,
                   const KParams &kp, const fcdemDistanceMap *map, float skin, unsigned *exact,
-                  const UmCount *count);
+                  const UmCount *count, int step);
 
 }  // namespace fcdem

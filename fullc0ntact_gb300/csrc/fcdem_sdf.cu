@@ -625,6 +625,19 @@ kSdfInfer(SdfView net, const float4 *__restrict__ pts, const int *__restrict__ s
   sdfTileTeardown<H, L>(sm);
 }
 
+// Per-tile hints of the culling kernels (performance only: results never
+// depend on them).  h[tile] = 1 when, the last time the network ran on the
+// tile, more than half of its in-box particles still needed the exact query;
+// such a tile then queries the map directly, without the network, until a
+// refresh step (every kHintRefresh steps) runs the network on every tile
+// again.  h == nullptr: the network runs on every tile with a particle in
+// the map box.
+constexpr unsigned kHintRefresh = 8;
+struct TileHints {
+  unsigned char *h;
+  int refresh;
+};
+
 // d_integrateSystem + d_checkBoundaryDistMap (kIntegrateDistMap's
 // arithmetic) with the map query skipped where the network predicts a
 // distance above `skin`: a point outside the map box reads 5.0 from the map
@@ -636,7 +649,8 @@ __global__ void __launch_bounds__(128)
 kIntegrateSdf(float4 *__restrict__ pos, float4 *__restrict__ vel, float dt, unsigned n,
               KParams kp, MapView M, SdfView net, float skin, unsigned *exact,
               unsigned *__restrict__ hashOut, unsigned *__restrict__ rankOut,
-              unsigned *__restrict__ cnt, unsigned *__restrict__ tileCnt, unsigned *status) {
+              unsigned *__restrict__ cnt, unsigned *__restrict__ tileCnt, TileHints hints,
+              unsigned *status) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   SdfTileSmem<H, L> &sm = *reinterpret_cast<SdfTileSmem<H, L> *>(smraw);
   sdfTileSetup<H, L>(sm, net);
@@ -657,16 +671,22 @@ kIntegrateSdf(float4 *__restrict__ pos, float4 *__restrict__ vel, float dt, unsi
     const bool inBox = valid && inMapBox(M, p);
     float dPred = 0.0f;
     // a tile with no particle in the map box needs no prediction (the map
-    // reads 5.0 outside its box); the decision is the same for every thread
-    if (__syncthreads_or(inBox) &&
+    // reads 5.0 outside its box); the decisions are the same for every thread
+    const bool anyIn = __syncthreads_or(inBox);
+    const bool useNet = anyIn && (!hints.h || hints.refresh || hints.h[tile] == 0);
+    if (useNet &&
         !sdfTileForward<H, L>(sm, net, (p.x - net.shift[0]) * net.scale[0],
                               (p.y - net.shift[1]) * net.scale[1],
                               (p.z - net.shift[2]) * net.scale[2], 0, phase, dPred)) {
       if (threadIdx.x == 0) atomicOr(status, (unsigned)kStatusTimeout);
       break;
     }
+    const bool test = inBox && (!useNet || !(dPred > skin));
+    if (useNet && hints.h) {
+      const int nIn = __syncthreads_count(inBox), nTest = __syncthreads_count(test);
+      if (threadIdx.x == 0) hints.h[tile] = 2 * nTest > nIn ? 1 : 0;
+    }
     if (!valid) continue;
-    const bool test = inBox && !(dPred > skin);
     if (test && exact) atomicAdd(exact, 1u);
     umBoundary(M, test, r, P.boundaryDamping, p, v);
     if (kCount) {  // the next step's calcHash and cell count
@@ -706,7 +726,7 @@ kBatchObstacle(const BatchScene *__restrict__ scenes, const unsigned *__restrict
                const MapView *__restrict__ maps, SdfView net, float skin,
                const float4 *__restrict__ inPos, float4 *__restrict__ pos,
                float4 *__restrict__ vel, float dt, unsigned n, UmCount count, int doCount,
-               unsigned *exact, unsigned *status) {
+               unsigned *exact, TileHints hints, unsigned *status) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   SdfTileSmem<H, L> &sm = *reinterpret_cast<SdfTileSmem<H, L> *>(smraw);
   if (kNet) sdfTileSetup<H, L>(sm, net);
@@ -730,8 +750,11 @@ kBatchObstacle(const BatchScene *__restrict__ scenes, const unsigned *__restrict
     if (shape >= 0) M = maps[shape];
     const bool inBox = shape >= 0 && inMapBox(M, p);
     float dPred = 0.0f;
+    bool useNet = false;
     if (kNet) {
-      if (__syncthreads_or(inBox) &&
+      const bool anyIn = __syncthreads_or(inBox);
+      useNet = anyIn && (!hints.h || hints.refresh || hints.h[tile] == 0);
+      if (useNet &&
           !sdfTileForward<H, L>(sm, net, (p.x - net.shift[0]) * net.scale[0],
                                 (p.y - net.shift[1]) * net.scale[1],
                                 (p.z - net.shift[2]) * net.scale[2], shape, phase, dPred)) {
@@ -739,8 +762,12 @@ kBatchObstacle(const BatchScene *__restrict__ scenes, const unsigned *__restrict
         break;
       }
     }
+    const bool test = inBox && (!useNet || !(dPred > skin));
+    if (kNet && useNet && hints.h) {
+      const int nIn = __syncthreads_count(inBox), nTest = __syncthreads_count(test);
+      if (threadIdx.x == 0) hints.h[tile] = 2 * nTest > nIn ? 1 : 0;
+    }
     if (!valid) continue;
-    const bool test = inBox && (!kNet || !(dPred > skin));
     if (test) {
       if (exact) atomicAdd(exact, 1u);
       checkDistMap(M, r, P.boundaryDamping, p, v);
@@ -787,6 +814,8 @@ struct fcdemSdfNet {
   __nv_bfloat16 *w16 = nullptr;
   bool w16Fresh = false;
   unsigned adamStep = 0;
+  unsigned char *hints = nullptr;  // per-tile culling hints (TileHints)
+  unsigned hintTiles = 0;
 };
 
 namespace fcdem {
@@ -819,6 +848,7 @@ void freeNet(fcdemSdfNet *net) {
   cudaFree(net->v);
   cudaFree(net->loss);
   cudaFree(net->w16);
+  cudaFree(net->hints);
   delete net;
 }
 
@@ -923,7 +953,7 @@ bool launchInfer(fcdemSdfNet *net, const float4 *pts, const int *shapes, unsigne
 template <int H, int L>
 bool launchIntegrateSdf(fcdemSdfNet *net, float4 *pos, float4 *vel, float dt, unsigned n,
                         const KParams &kp, const MapView &M, float skin, unsigned *exact,
-                        const UmCount *count) {
+                        const UmCount *count, TileHints hints) {
   const size_t smem = tileSmemBytes<H, L>();
   unsigned grid = (n + 127) / 128;
   if (grid > 152u * sdfCtasPerSm<H, L>()) grid = 152u * sdfCtasPerSm<H, L>();
@@ -932,13 +962,13 @@ bool launchIntegrateSdf(fcdemSdfNet *net, float4 *pos, float4 *vel, float dt, un
                          (int)smem);
     kIntegrateSdf<H, L, true><<<grid, 128, smem, curStream()>>>(
         pos, vel, dt, n, kp, M, sdfView(net), skin, exact, count->hash, count->rank, count->cnt,
-        count->tileCnt, ctx().dStatus);
+        count->tileCnt, hints, ctx().dStatus);
   } else {
     cudaFuncSetAttribute(kIntegrateSdf<H, L, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
     kIntegrateSdf<H, L, false><<<grid, 128, smem, curStream()>>>(
         pos, vel, dt, n, kp, M, sdfView(net), skin, exact, nullptr, nullptr, nullptr, nullptr,
-        ctx().dStatus);
+        hints, ctx().dStatus);
   }
   return launchOk();
 }
@@ -947,7 +977,7 @@ template <int H, int L, bool kNet, bool kW>
 bool launchBatchObstacle(fcdemSdfNet *net, const BatchScene *scenes, const unsigned *sceneOf,
                          const MapView *maps, float skin, const float4 *inPos, float4 *pos,
                          float4 *vel, float dt, unsigned n, const UmCount *count,
-                         unsigned *exact) {
+                         unsigned *exact, TileHints hints) {
   unsigned grid = (n + 127) / 128;
   size_t smem = 0;
   SdfView v{};
@@ -960,7 +990,7 @@ bool launchBatchObstacle(fcdemSdfNet *net, const BatchScene *scenes, const unsig
   }
   kBatchObstacle<H, L, kNet, kW><<<grid, 128, smem, curStream()>>>(
       scenes, sceneOf, maps, v, skin, inPos, pos, vel, dt, n, count ? *count : UmCount{},
-      count ? 1 : 0, exact, ctx().dStatus);
+      count ? 1 : 0, exact, hints, ctx().dStatus);
   return launchOk();
 }
 
@@ -969,28 +999,49 @@ bool launchBatchObstacle(fcdemSdfNet *net, const BatchScene *scenes, const unsig
 
 namespace fcdem {
 
+// The net's hint array for `tiles` tiles (grown on demand, cleared when
+// grown); nullptr (no hints) when it cannot be had.
+unsigned char *sdfHints(fcdemSdfNet *net, unsigned tiles) {
+  if (net->hints && net->hintTiles >= tiles) return net->hints;
+  if (!cudaOk(cudaDeviceSynchronize())) return nullptr;
+  cudaFree(net->hints);
+  net->hints = nullptr;
+  net->hintTiles = 0;
+  if (cudaMalloc(&net->hints, tiles) != cudaSuccess) {
+    cudaGetLastError();
+    net->hints = nullptr;
+    return nullptr;
+  }
+  if (!cudaOk(cudaMemset(net->hints, 0, tiles))) return nullptr;
+  net->hintTiles = tiles;
+  return net->hints;
+}
+
 bool batchObstacleIntegrate(const BatchScene *scenes, const unsigned *sceneOf, bool radiusFromW,
                             const MapView *maps, fcdemSdfNet *net, float skin,
                             const float4 *inPos, float4 *pos, float4 *vel, float dt,
-                            unsigned n, const UmCount *count, unsigned *exact) {
+                            unsigned n, const UmCount *count, unsigned *exact, unsigned step) {
   if (n == 0) return true;
   if (!net) {
+    const TileHints none{nullptr, 1};
     return radiusFromW
                ? launchBatchObstacle<64, 3, false, true>(net, scenes, sceneOf, maps, skin, inPos,
-                                                         pos, vel, dt, n, count, exact)
+                                                         pos, vel, dt, n, count, exact, none)
                : launchBatchObstacle<64, 3, false, false>(net, scenes, sceneOf, maps, skin,
-                                                          inPos, pos, vel, dt, n, count, exact);
+                                                          inPos, pos, vel, dt, n, count, exact,
+                                                          none);
   }
   if (!packWeights(net)) return false;
+  const TileHints hints{sdfHints(net, (n + 127) / 128), step % kHintRefresh == 0 ? 1 : 0};
   const int H = net->lay.H, L = net->lay.L;
 #define FCDEM_BATCH_OBST(HH, LL)                                                             \
   if (H == HH && L == LL)                                                                    \
     return radiusFromW ? launchBatchObstacle<HH, LL, true, true>(net, scenes, sceneOf, maps, \
                                                                  skin, inPos, pos, vel, dt,  \
-                                                                 n, count, exact)            \
+                                                                 n, count, exact, hints)     \
                        : launchBatchObstacle<HH, LL, true, false>(                           \
                              net, scenes, sceneOf, maps, skin, inPos, pos, vel, dt, n,       \
-                             count, exact);
+                             count, exact, hints);
   FCDEM_BATCH_OBST(64, 3)
   FCDEM_BATCH_OBST(64, 2)
   FCDEM_BATCH_OBST(128, 2)
@@ -1002,14 +1053,17 @@ bool batchObstacleIntegrate(const BatchScene *scenes, const unsigned *sceneOf, b
 
 bool sdfIntegrate(fcdemSdfNet *net, float4 *pos, float4 *vel, float dt, unsigned n,
                   const KParams &kp, const fcdemDistanceMap *map, float skin, unsigned *exact,
-                  const UmCount *count) {
+                  const UmCount *count, int step) {
   if (!packWeights(net)) return false;
   const int H = net->lay.H, L = net->lay.L;
   const MapView M = view(map);
-  if (H == 64 && L == 3) return launchIntegrateSdf<64, 3>(net, pos, vel, dt, n, kp, M, skin, exact, count);
-  if (H == 64 && L == 2) return launchIntegrateSdf<64, 2>(net, pos, vel, dt, n, kp, M, skin, exact, count);
-  if (H == 128 && L == 2) return launchIntegrateSdf<128, 2>(net, pos, vel, dt, n, kp, M, skin, exact, count);
-  if (H == 128 && L == 3) return launchIntegrateSdf<128, 3>(net, pos, vel, dt, n, kp, M, skin, exact, count);
+  // step < 0: a lone call, no hints
+  const TileHints hints{step < 0 ? nullptr : sdfHints(net, (n + 127) / 128),
+                        (step < 0 || step % (int)kHintRefresh == 0) ? 1 : 0};
+  if (H == 64 && L == 3) return launchIntegrateSdf<64, 3>(net, pos, vel, dt, n, kp, M, skin, exact, count, hints);
+  if (H == 64 && L == 2) return launchIntegrateSdf<64, 2>(net, pos, vel, dt, n, kp, M, skin, exact, count, hints);
+  if (H == 128 && L == 2) return launchIntegrateSdf<128, 2>(net, pos, vel, dt, n, kp, M, skin, exact, count, hints);
+  if (H == 128 && L == 3) return launchIntegrateSdf<128, 3>(net, pos, vel, dt, n, kp, M, skin, exact, count, hints);
   setError(FCDEM_ERR_INVALID_VALUE);
   return false;
 }
@@ -1201,7 +1255,7 @@ void fcdemUM_integrateSystemSdf(float *pos, float *vel, float deltaTime, uint nu
     return;
   }
   sdfIntegrate(net, (float4 *)pos, (float4 *)vel, deltaTime, numParticles, kparams(c), map, skin,
-               exactQueries, nullptr);
+               exactQueries, nullptr, -1);
 }
 
 }  // extern "C"

@@ -384,7 +384,7 @@ void fcdemUM_update(float *pos, float *vel, float *force, float *sortedPos, floa
     stageBegin(0);
     if (net)
       ok = sdfIntegrate(net, (float4 *)pos, (float4 *)vel, deltaTime, n, kp, map, skin,
-                        exactQueries, last ? nullptr : &count);
+                        exactQueries, last ? nullptr : &count, (int)s);
     else
       ok = mapIntegrate((float4 *)pos, (float4 *)vel, deltaTime, n, kp, map,
                         last ? nullptr : &count);
