@@ -63,21 +63,21 @@ def parse():
                     help="skip the batched-scenes measurement")
     ap.add_argument("--cell-order", choices=["linear", "morton"], default="linear",
                     help="cell keys of the headline job (results are identical)")
-    ap.add_argument("--no-config2", action="store_true",
+    ap.add_argument("--no-torus", action="store_true",
                     help="skip the torus-obstacle (distance map / neural SDF) measurement")
-    ap.add_argument("--config2-n", type=int, default=1048576)
-    ap.add_argument("--config2-steps", type=int, default=200)
-    ap.add_argument("--no-config4", action="store_true",
+    ap.add_argument("--torus-n", type=int, default=1048576)
+    ap.add_argument("--torus-steps", type=int, default=200)
+    ap.add_argument("--no-obstacle-batch", action="store_true",
                     help="skip the batched scenes with obstacles and the shape network")
-    ap.add_argument("--config4-scenes", type=int, default=128)
-    ap.add_argument("--config4-steps", type=int, default=500)
+    ap.add_argument("--obstacle-scenes", type=int, default=128)
+    ap.add_argument("--obstacle-steps", type=int, default=500)
     ap.add_argument("--batch-scenes", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=20)
     return ap.parse_args()
 
 
 def load_scene(n: int) -> dict:
-    """config1 scene, cached on local disk (packing 4M spheres takes ~15 s)."""
+    """The packed 4,194,304-sphere scene, cached on local disk (packing 4M spheres takes ~15 s)."""
     from fullc0ntact_gb300 import scenes
     from fullc0ntact_gb300.params import SimParams
     path = os.path.join(tempfile.gettempdir(), f"fcdem_scene_packed_{n}_v2.npz")
@@ -89,7 +89,7 @@ def load_scene(n: int) -> dict:
                             radius_from_w=True, dt=float(z["dt"]))
         except Exception:
             pass
-    sc = scenes.config1(n)
+    sc = scenes.packed_scene(n)
     tmp = path + f".{os.getpid()}.tmp.npz"
     np.savez(tmp, name=sc["name"], pos=sc["pos"], vel=sc["vel"],
              params=np.frombuffer(bytes(sc["params"]), np.uint8), dt=sc["dt"])
@@ -194,7 +194,7 @@ def load_batch(num_scenes: int) -> list:
                 return out
         except Exception:
             pass
-    sl = scenes.batch_config3(num_scenes)
+    sl = scenes.batch_box_scenes(num_scenes)
     arrays = {"k": np.int64(len(sl))}
     for i, sc in enumerate(sl):
         arrays[f"pos{i}"] = sc["pos"]
@@ -260,7 +260,7 @@ def measured_peak_tflops():
         return 1900.0, "fallback"
 
 
-def measure_config2(n: int, steps: int, dev: int) -> dict:
+def measure_torus_obstacle(n: int, steps: int, dev: int) -> dict:
     """Spheres falling onto the torus obstacle (128^3 distance map) through
     the fused unified-memory step: plain (exact map query for every particle
     in the map box) and with the neural SDF culling the query (3 -> 64 -> 64
@@ -286,7 +286,7 @@ def measure_config2(n: int, steps: int, dev: int) -> dict:
     del train
     # judge: the exact map on held-out samples
     val = sdf.samples(dmap, 1_048_576, 0.5, 0.03, seed=99)
-    sc = scenes.config2(n)
+    sc = scenes.torus_fall_scene(n)
     r = sc["radius"]
     skin = 2.0 * r
     pred = net.infer(val)
@@ -329,7 +329,7 @@ def measure_config2(n: int, steps: int, dev: int) -> dict:
         e1.record()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
-        dem.check(f"config2 {mode}")
+        dem.check(f"torus obstacle {mode}")
         finals[mode] = (us.pos.clone(), us.vel.clone())
         exact = int(counter.item())
         # stage attribution over the same steps
@@ -341,7 +341,7 @@ def measure_config2(n: int, steps: int, dev: int) -> dict:
         cnt = (C.c_uint * 5)()
         lib.fcdemGetStageTimes(st, cnt, 5)
         lib.fcdemSetProfiling(0)
-        dem.check(f"config2 {mode} stages")
+        dem.check(f"torus obstacle {mode} stages")
         names = ["integrate_hash", "sort", "tables", "reorder", "collide"]
         out[mode] = {"value": n * steps / (ms / 1e3), "ms_per_step": ms / steps,
                      "stage_ms_per_step": {names[k]: (st[k] / steps if cnt[k] else None)
@@ -369,7 +369,7 @@ def measure_config2(n: int, steps: int, dev: int) -> dict:
                                       "frac": tc_flop / (infer_ms / 1e3) / 1e12 / peak_tf}}
 
 
-def measure_config4(num_scenes: int, steps: int, dev: int) -> dict:
+def measure_batched_obstacles(num_scenes: int, steps: int, dev: int) -> dict:
     """Batched + neural SDF: scenes with sizes log-uniform in [4096, 262144],
     each over one of 8 procedural obstacles (128-cell maps); one
     shape-conditioned network (11 -> 128 -> 128 -> 1) trained on samples of
@@ -379,7 +379,7 @@ def measure_config4(num_scenes: int, steps: int, dev: int) -> dict:
     queries (the plain step)."""
     import torch
     from fullc0ntact_gb300 import dem, scenes, sdf
-    scs, obs, shape = scenes.batch_config4(num_scenes)
+    scs, obs, shape = scenes.batch_obstacle_scenes(num_scenes)
     n_total = sum(s["pos"].shape[0] for s in scs)
     maps = sdf.obstacle_maps(obs, 128)
     torch.cuda.synchronize()
@@ -413,7 +413,7 @@ def measure_config4(num_scenes: int, steps: int, dev: int) -> dict:
         b.update(steps, graph=True)
         e1.record()
         torch.cuda.synchronize()
-        dem.check("config4 batch")
+        dem.check("obstacle batch")
         return b, e0.elapsed_time(e1), b.exact_queries()
 
     bn, ms_n, ex_n = timed_batch(True)
@@ -436,7 +436,7 @@ def measure_config4(num_scenes: int, steps: int, dev: int) -> dict:
         one.update(steps, graph=False)
     e1.record()
     torch.cuda.synchronize()
-    dem.check("config4 per scene")
+    dem.check("obstacle scene alone")
     ms_s = e0.elapsed_time(e1)
     del singles
     torch.cuda.empty_cache()
@@ -683,14 +683,14 @@ def run_ours(args):
     clk = clocks.stop()
 
     lib.fcdemSetCellOrder(0)
-    config2 = None
-    if not args.no_config2:
-        config2 = measure_config2(args.config2_n, args.config2_steps, dev)
+    torus_obstacle = None
+    if not args.no_torus:
+        torus_obstacle = measure_torus_obstacle(args.torus_n, args.torus_steps, dev)
         torch.cuda.empty_cache()
 
-    config4 = None
-    if not args.no_config4:
-        config4 = measure_config4(args.config4_scenes, args.config4_steps, dev)
+    batched_obstacles = None
+    if not args.no_obstacle_batch:
+        batched_obstacles = measure_batched_obstacles(args.obstacle_scenes, args.obstacle_steps, dev)
         torch.cuda.empty_cache()
 
     batched = None
@@ -729,8 +729,8 @@ def run_ours(args):
             "phases": phases,
             "final_cells": final_cells,
             "batched": batched,
-            "config2": config2,
-            "config4": config4,
+            "torus_obstacle": torus_obstacle,
+            "batched_obstacles": batched_obstacles,
             "clocks": clk,
             "cpu_baseline": cpu,
         }

@@ -50,7 +50,7 @@ def pack(n: int, box_min, box_max, r_median: float, sigma: float, r_max: float,
     return pos, vel
 
 
-def config0(n: int = 16384, seed: int = 1973) -> dict:
+def lattice_scene(n: int = 16384, seed: int = 1973) -> dict:
     """Plain DEM: n monodisperse spheres of radius 1/64 on a jittered lattice
     (spacing 2r, jitter 0.01r) in the [-1,1]^3 box, 64^3 grid with cell = 2r,
     velocities U[-0.01, 0.01], gravity -3e-4, spring 0.5, damping 0.02,
@@ -65,12 +65,12 @@ def lognormal_mean_volume(r_median: float, sigma: float) -> float:
     return 4.0 / 3.0 * math.pi * r_median ** 3 * math.exp(4.5 * sigma * sigma)
 
 
-def config1(n: int = 4194304, seed: int = 2024, grid: int = 256,
+def packed_scene(n: int = 4194304, seed: int = 2024, grid: int = 256,
             volume_fraction: float = 0.30) -> dict:
     """Plain DEM at scale: n spheres with lognormal radii (median 1/512,
     sigma 0.25, clipped at 2/512), cell = max diameter (grid cells span the
     [-1,1] box), random sequential packing at the given volume fraction in a
-    centred cube, same contact parameters as config0.  Smaller n keep the
+    centred cube, the contact parameters of lattice_scene.  Smaller n keep the
     radii and the packing density (the cube shrinks)."""
     r_med, sigma, r_max = 1.0 / 512.0, 0.25, 2.0 / 512.0
     vol = n * lognormal_mean_volume(r_med, sigma)
@@ -86,12 +86,12 @@ def config1(n: int = 4194304, seed: int = 2024, grid: int = 256,
                 radius_from_w=True, dt=0.5, box_side=side)
 
 
-def config2(n: int = 1048576, seed: int = 2, grid: int = 256, z0: float = 0.15) -> dict:
+def torus_fall_scene(n: int = 1048576, seed: int = 2, grid: int = 256, z0: float = 0.15) -> dict:
     """Spheres falling onto a torus (the distance-map obstacle): n spheres of
     radius 1/256 on a jittered lattice (spacing 2.2 r, jitter 0.05 r),
     128 x 128 columns wide, centred over the torus (R 0.3, r 0.1, in the
     z = 0 plane) and starting at z = z0; velocities U[-0.001, 0.001];
-    gravity -3e-4 along z, the config0 contact parameters, dt 0.5; grid^3
+    gravity -3e-4 along z, the contact parameters of lattice_scene, dt 0.5; grid^3
     cells of one diameter from (-1, -1, -1); no collider sphere (the
     unified-memory evalForces has none)."""
     r = 1.0 / 256.0
@@ -176,7 +176,7 @@ def batch_scene(n: int, seed: int, volume_fraction: float = 0.25, r_min: float =
                 dt=0.5, box_lo=np.array(lo, np.float32), box_hi=np.array(hi, np.float32))
 
 
-def batch_config3(num_scenes: int = 512, n_min: int = 1024, n_max: int = 65536,
+def batch_box_scenes(num_scenes: int = 512, n_min: int = 1024, n_max: int = 65536,
                   seed: int = 3) -> list:
     """Batched plain DEM: scene sizes drawn log-uniform in [n_min, n_max]
     (seeded), radii U[1/512, 1/256], 25% volume fraction per scene."""
@@ -212,7 +212,7 @@ def obstacle_scene(n: int, ob: dict, seed: int, r_min: float = 1.0 / 512.0,
     U[r_min, r_max] on a jittered lattice (spacing 2.05 r_max, at most
     120 x 120 columns) starting one diameter above the obstacle's top,
     falling (gravity -3e-4 along z) onto it inside the box [-0.5, 0.5]^3;
-    128^3 grid cells of one max diameter; config0 contact parameters."""
+    128^3 grid cells of one max diameter; the contact parameters of lattice_scene."""
     rng = np.random.default_rng(seed)
     sp = 2.05 * r_max
     nx = ny = min(120, max(1, int(np.ceil(np.sqrt(n)))))
@@ -234,7 +234,7 @@ def obstacle_scene(n: int, ob: dict, seed: int, r_min: float = 1.0 / 512.0,
                 box_hi=np.array([0.5] * 3, np.float32))
 
 
-def batch_config4(num_scenes: int = 128, n_min: int = 4096, n_max: int = 262144,
+def batch_obstacle_scenes(num_scenes: int = 128, n_min: int = 4096, n_max: int = 262144,
                   seed: int = 4, num_shapes: int = 8):
     """Batched DEM with obstacles: scene sizes log-uniform in [n_min, n_max]
     (seeded), scene s over obstacle s % num_shapes.  Returns (scenes,

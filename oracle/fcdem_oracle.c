@@ -1,8 +1,9 @@
 /*
  * fcdem_oracle.c -- CPU restatement of FullC0ntact's particle-DEM step.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the GPU kernels.  Only tests/,
- * the smoke check and the CPU-baseline leg of bench.py load it.
+ * TEST INFRASTRUCTURE ONLY: the CPU restatement the GPU kernels are tested
+ * against.  Only tests/, the smoke check and the CPU-baseline leg of bench.py
+ * load it.
  *
  * Build with -ffp-contract=off (see oracle/Makefile): every a*b+c below is
  * two roundings, on every host architecture.

@@ -1,9 +1,9 @@
 /*
  * fcdem_oracle.h -- CPU restatement of FullC0ntact's particle-DEM step.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker for the GPU
- * implementation: only the test suite, the smoke check and the CPU-baseline
- * leg of the benchmark load it.  The product library never links or calls it.
+ * TEST INFRASTRUCTURE ONLY.  The tests compare the GPU implementation
+ * against this library: only the test suite, the smoke check and the
+ * CPU-baseline leg of the benchmark load it.  The product library never links or calls it.
  *
  * Every function restates one routine of the reference in plain C with the
  * same operation order, compiled with -ffp-contract=off so that results are

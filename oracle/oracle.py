@@ -1,8 +1,8 @@
 """ctypes bindings of the CPU oracle (TEST INFRASTRUCTURE ONLY).
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` import this module: it is the checker for the CUDA kernels of
-``fullc0ntact_gb300``, never part of the product path.
+``bench.py`` import this module: the CUDA kernels of ``fullc0ntact_gb300``
+are tested against it; it is never part of the product path.
 
 Three libraries are wrapped:
 

@@ -89,7 +89,7 @@ def run_reference(P, pos0, vel0, dt):
 def cases():
     rng = np.random.default_rng(20241203)
     out = {}
-    # config 0 of the benchmark set: 16384 spheres r = 1/64 on the jittered
+    # the lattice scene: 16384 spheres r = 1/64 on the jittered
     # lattice, 64^3 grid.
     r = 1.0 / 64.0
     pos, vel = lattice(16384, r, 0.01 * r, 0.01, rng)

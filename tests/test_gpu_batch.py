@@ -44,7 +44,7 @@ def test_graph_replays_repeatedly():
 
 def test_one_scene_batch_in_unit_box_equals_update():
     from fullc0ntact_gb300 import dem, scenes
-    sc = scenes.config1(30000, grid=128)
+    sc = scenes.packed_scene(30000, grid=128)
     sc["box_lo"] = np.array([-1.0, -1.0, -1.0], np.float32)
     sc["box_hi"] = np.array([1.0, 1.0, 1.0], np.float32)
     b = dem.Batch([sc])

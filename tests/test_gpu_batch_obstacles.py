@@ -32,15 +32,15 @@ def test_rounded_box_generator_matches_analytic():
     assert np.abs(np.abs(v[:, 0]) - dd).max() <= 2e-6
 
 
-def _small_config4(num_scenes=6, n_min=3000, n_max=20000, seed=5):
+def _small_obstacle_batch(num_scenes=6, n_min=3000, n_max=20000, seed=5):
     from fullc0ntact_gb300 import scenes
-    return scenes.batch_config4(num_scenes, n_min, n_max, seed=seed, num_shapes=4)
+    return scenes.batch_obstacle_scenes(num_scenes, n_min, n_max, seed=seed, num_shapes=4)
 
 
 @pytest.mark.parametrize("graph", [False, True])
 def test_obstacle_batch_equals_each_scene_alone(graph):
     from fullc0ntact_gb300 import dem, sdf
-    scs, obs, shape = _small_config4()
+    scs, obs, shape = _small_obstacle_batch()
     maps = sdf.obstacle_maps(obs, 64)
     b = dem.Batch(scs)
     b.set_obstacles(maps, shape)
@@ -60,7 +60,7 @@ def test_obstacle_batch_equals_each_scene_alone(graph):
 
 def test_shape_network_judged_by_maps_and_culling_is_exact():
     from fullc0ntact_gb300 import dem, sdf
-    scs, obs, shape = _small_config4(num_scenes=8, seed=6)
+    scs, obs, shape = _small_obstacle_batch(num_scenes=8, seed=6)
     maps = sdf.obstacle_maps(obs, 128)
     net, loss = sdf.shape_net(maps)
     print("shape net loss", loss)

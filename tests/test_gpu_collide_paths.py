@@ -25,9 +25,9 @@ def _run(sc, path, steps):
 def test_tiled_equals_global(case):
     from fullc0ntact_gb300 import scenes
     if case == "packed":
-        sc = scenes.config1(200_000, grid=128)
+        sc = scenes.packed_scene(200_000, grid=128)
     elif case == "lattice":
-        sc = scenes.config0(16384)
+        sc = scenes.lattice_scene(16384)
     elif case == "wrap":  # particles across the whole x range: windows wrap
         sc = scenes.random_box(30000, grid=(32, 32, 32), radius=1.0 / 32.0, seed=8)
     elif case == "random_poly":
@@ -58,9 +58,9 @@ def _run_cull(sc, on, steps):
 def test_cell_culling_is_exact(case):
     from fullc0ntact_gb300 import scenes
     if case == "packed":
-        sc = scenes.config1(200_000, grid=128)
+        sc = scenes.packed_scene(200_000, grid=128)
     elif case == "lattice":
-        sc = scenes.config0(16384)
+        sc = scenes.lattice_scene(16384)
     elif case == "wrap":
         sc = scenes.random_box(30000, grid=(32, 32, 32), radius=1.0 / 64.0, seed=8)
     elif case == "random_poly":  # particleRadius bounds the radii in w
@@ -92,7 +92,7 @@ def _crowded_scene(kind):
     elif kind == "poly":
         sc = scenes.random_box(20000, grid=(16, 16, 16), radius=1.0 / 16.0, seed=22, poly=True)
     else:  # packed polydisperse scene with three collapsed cells
-        sc = scenes.config1(100_000, grid=128)
+        sc = scenes.packed_scene(100_000, grid=128)
     rng = np.random.default_rng(23)
     cell = float(sc["params"].cellSize[0])
     origin = np.array([sc["params"].worldOrigin[k] for k in range(3)], np.float32)

@@ -29,7 +29,7 @@ def test_mesh_map_matches_fp64_oracle():
     assert np.abs(on).max() <= 2e-6
 
 
-def test_config2_mesh_map_matches_exact_torus():
+def test_torus_mesh_map_matches_exact_torus():
     from fullc0ntact_gb300 import dem, scenes
     R, r = 0.3, 0.1
     verts, tris = scenes.torus_mesh(R, r, 256, 64)

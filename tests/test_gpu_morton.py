@@ -38,7 +38,7 @@ def _same_bits(a, b):
 @pytest.mark.parametrize("kind", ["lattice", "packed"])
 def test_staged_stages_morton_vs_linear(kind):
     from fullc0ntact_gb300 import dem, scenes
-    sc = scenes.config0(16384) if kind == "lattice" else scenes.config1(100_000, grid=128)
+    sc = scenes.lattice_scene(16384) if kind == "lattice" else scenes.packed_scene(100_000, grid=128)
 
     def stages(sc):
         ds = dem.DeviceScene(sc)
@@ -79,7 +79,7 @@ def test_staged_stages_morton_vs_linear(kind):
 @pytest.mark.parametrize("pipeline", [0, 1])
 def test_fused_update_morton_vs_linear(pipeline):
     from fullc0ntact_gb300 import dem, scenes
-    sc = scenes.config1(200_000, grid=128)
+    sc = scenes.packed_scene(200_000, grid=128)
 
     def upd(sc):
         dem.lib.fcdemSetUpdatePipeline(pipeline)
@@ -98,7 +98,7 @@ def test_fused_update_morton_vs_linear(pipeline):
 def test_um_update_with_map_and_crowded_cells_morton_vs_linear():
     from fullc0ntact_gb300 import dem, scenes
     dmap = dem.DistanceMap.torus(0.3, 0.1, 128, 0.05)
-    sc = scenes.config2(80_000, z0=0.09)
+    sc = scenes.torus_fall_scene(80_000, z0=0.09)
     # a collapsed cell and its neighbourhood (the crowd path)
     rng = np.random.default_rng(3)
     idx = rng.permutation(sc["pos"].shape[0])[:3000]

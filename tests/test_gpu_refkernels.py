@@ -58,12 +58,12 @@ def _run_ref(R, P, pos0, vel0, dt):
                 nv=nv.cpu().numpy())
 
 
-@pytest.mark.parametrize("which", ["config0", "random", "wrap"])
+@pytest.mark.parametrize("which", ["lattice", "random", "wrap"])
 def test_product_matches_reference_kernels(which):
     from fullc0ntact_gb300 import dem, scenes
     R = _ref()
-    if which == "config0":
-        sc = scenes.config0()
+    if which == "lattice":
+        sc = scenes.lattice_scene()
     elif which == "random":
         sc = scenes.random_box(20000, grid=(32, 32, 32), radius=1.0 / 32.0, seed=4)
     else:

@@ -31,7 +31,7 @@ def test_um_update_equals_staged(steps, with_map):
     from fullc0ntact_gb300 import dem, scenes
     dmap = dem.DistanceMap.torus(0.3, 0.1, 128, 0.05) if with_map else None
     # the lowest layers start in and just above the torus: the map pushes
-    sc = scenes.config2(60_000, z0=0.09)
+    sc = scenes.torus_fall_scene(60_000, z0=0.09)
     a, b = dem.UmScene(sc, dmap), dem.UmScene(sc, dmap)
     for _ in range(steps):
         a.stages()
@@ -47,7 +47,7 @@ def test_um_update_with_sdf_culling_equals_exact_map():
     net.normalize_to(dmap)
     net.train(sdf.samples(dmap, 2_000_000, 0.6, 0.05, seed=21), epochs=20, batch=2048,
               lr=5e-3, band=0.02)
-    sc = scenes.config2(200_000, z0=0.105)
+    sc = scenes.torus_fall_scene(200_000, z0=0.105)
     r = sc["radius"]
     a, b = dem.UmScene(sc, dmap), dem.UmScene(sc, dmap)
     counter = torch.zeros(1, dtype=torch.int32, device="cuda")

@@ -24,7 +24,7 @@ def test_fused_update_equals_staged(pipeline, poly, steps):
     counting sort with stable fix-up) against the five staged calls."""
     from fullc0ntact_gb300 import dem, scenes
     sc = (scenes.random_box(5000, grid=(32, 32, 32), radius=1.0 / 24.0, seed=3, poly=True)
-          if poly else scenes.config0(4096))
+          if poly else scenes.lattice_scene(4096))
     a, b = dem.DeviceScene(sc), dem.DeviceScene(sc)
     for _ in range(steps):
         a.stages()
@@ -81,7 +81,7 @@ def test_multistep_statistics_match_oracle():
     momentum and contact count, not particle by particle."""
     from fullc0ntact_gb300 import dem, scenes
     from oracle import oracle as O
-    sc = scenes.config0(8192)
+    sc = scenes.lattice_scene(8192)
     ds = dem.DeviceScene(sc)
     ds.update(50)
     dem.check()
@@ -107,7 +107,7 @@ def test_multistep_statistics_match_oracle():
 
 def test_stream_selection():
     from fullc0ntact_gb300 import dem, scenes
-    sc = scenes.config0(2048)
+    sc = scenes.lattice_scene(2048)
     a, b = dem.DeviceScene(sc), dem.DeviceScene(sc)
     a.update(3)
     s = torch.cuda.Stream()
@@ -126,7 +126,7 @@ def test_counting_pipeline_on_packed_scene_and_crowded_cells():
     (40 particles in one cell) and on a packed polydisperse scene."""
     from fullc0ntact_gb300 import dem, scenes
     for sc in (scenes.random_box(3000, grid=(8, 8, 8), radius=0.02, cell=0.25, seed=4),
-               scenes.config1(100_000, grid=128)):
+               scenes.packed_scene(100_000, grid=128)):
         sc["pos"][:40, :3] = 0.01 + 0.001 * np.arange(40, dtype=np.float32)[:, None]
         a, b = dem.DeviceScene(sc), dem.DeviceScene(sc)
         for _ in range(3):
@@ -147,7 +147,7 @@ def test_counting_pipeline_cells_above_rerank_limit(n, grid):
     if grid == 8:
         sc = scenes.random_box(n, grid=(8, 8, 8), radius=0.02, cell=0.25, seed=11)
     else:
-        sc = scenes.config1(n, grid=grid)
+        sc = scenes.packed_scene(n, grid=grid)
     rng = np.random.default_rng(5)
     cell = float(sc["params"].cellSize[0])
     origin = np.array([sc["params"].worldOrigin[k] for k in range(3)], np.float32)

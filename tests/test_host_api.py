@@ -61,7 +61,7 @@ int main() {
 
 def test_packing_has_no_overlaps_and_reaches_density():
     from fullc0ntact_gb300 import scenes
-    sc = scenes.config1(20000, grid=64)
+    sc = scenes.packed_scene(20000, grid=64)
     p = sc["pos"].astype(np.float64)
     r = p[:, 3]
     assert r.max() <= 2.0 / 512.0 + 1e-9 and r.min() > 0
@@ -77,7 +77,7 @@ def test_packing_has_no_overlaps_and_reaches_density():
 
 def test_scene_generators_are_deterministic():
     from fullc0ntact_gb300 import scenes
-    a, b = scenes.config0(1000), scenes.config0(1000)
+    a, b = scenes.lattice_scene(1000), scenes.lattice_scene(1000)
     np.testing.assert_array_equal(a["pos"], b["pos"])
-    c, d = scenes.config1(3000, grid=32), scenes.config1(3000, grid=32)
+    c, d = scenes.packed_scene(3000, grid=32), scenes.packed_scene(3000, grid=32)
     np.testing.assert_array_equal(c["pos"], d["pos"])
