@@ -535,11 +535,13 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded packing)",
-        "config": {"workload": WORKLOAD, "n": n, "grid": 256, "l2": "inputs larger than L2"},
+        "config": {"workload": f"{WORKLOAD}, {args.steps}-step job from the packed state",
+                   "n": n, "grid": 256, "l2": "inputs larger than L2 (no flush)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{steps} of {args.steps} steps timed, each a full update "
                                    f"of the {n}-sphere scene (collide on {threads} threads, "
-                                   f"other stages on 1)"},
+                                   f"other stages on 1), from the start of the job: the "
+                                   f"cheapest steps of it (later ones hold crowded cells)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
