@@ -230,6 +230,39 @@ kMeshMap(float4 *__restrict__ vert, int vx, int vy, int vz, float3 vmin, float c
   vert[t] = make_float4(inside ? -d : d, bestCp.x, bestCp.y, bestCp.z);
 }
 
+// d_integrateRigidBody (particledem_um.cu:640-718), one thread per body:
+// the body's velocity takes gravity and the global damping, its centre moves
+// by v dt; of both, only z is stored (the reference writes vel_.z and com_.z
+// and nothing else), and the body's member particles are translated by the
+// full v dt with w = 1.  The reference's box clamp acts on its local copies
+// after the stores and changes nothing; it is left out.  The reference moves
+// particles 0..2 for body 0 and 3..5 for every other body; here each body
+// moves the members listed in its own indices[0 .. numParticles).
+__global__ void __launch_bounds__(128)
+kIntegrateRigidBodies(fcdemRigidBody *__restrict__ bodies, unsigned nb,
+                      float4 *__restrict__ pos, unsigned np, float dt, KParams kp) {
+  const unsigned b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  const SimParams &P = kp.p;
+  fcdemRigidBody rb = bodies[b];
+  float3 v = make_float3(rb.vel[0], rb.vel[1], rb.vel[2]);
+  v.x = fmaf(P.gravity[0], dt, v.x);
+  v.y = fmaf(P.gravity[1], dt, v.y);
+  v.z = fmaf(P.gravity[2], dt, v.z);
+  v.x = __fmul_rn(v.x, P.globalDamping);
+  v.y = __fmul_rn(v.y, P.globalDamping);
+  v.z = __fmul_rn(v.z, P.globalDamping);
+  bodies[b].vel[2] = v.z;
+  bodies[b].com[2] = fmaf(v.z, dt, rb.com[2]);
+  const int m = rb.numParticles < 3 ? rb.numParticles : 3;
+  for (int k = 0; k < m; ++k) {
+    const int q = rb.indices[k];
+    if (q < 0 || (unsigned)q >= np) continue;
+    const float4 p = pos[q];
+    pos[q] = make_float4(fmaf(v.x, dt, p.x), fmaf(v.y, dt, p.y), fmaf(v.z, dt, p.z), 1.0f);
+  }
+}
+
 }  // namespace
 }  // namespace fcdem
 
@@ -464,6 +497,17 @@ void fcdemUM_integrateSystem(float *pos, float *vel, float deltaTime, uint numPa
   if (numParticles == 0) return;
   if (!pos || !vel) { setError(FCDEM_ERR_INVALID_VALUE); return; }
   mapIntegrate((float4 *)pos, (float4 *)vel, deltaTime, numParticles, kparams(c), map, nullptr);
+}
+
+void fcdemUM_integrateRigidBodies(fcdemRigidBody *bodies, uint numBodies, float *pos,
+                                  uint numParticles, float deltaTime) {
+  Context &c = ctx();
+  if (!c.haveParams) { setError(FCDEM_ERR_NO_PARAMS); return; }
+  if (numBodies == 0) return;
+  if (!bodies || !pos) { setError(FCDEM_ERR_INVALID_VALUE); return; }
+  kIntegrateRigidBodies<<<(numBodies + 127) / 128, 128, 0, curStream()>>>(
+      bodies, numBodies, (float4 *)pos, numParticles, deltaTime, kparams(c));
+  launchOk();
 }
 
 void fcdemUM_evalForces(float *newVel, float *force, float *sortedPos, float *sortedVel,

@@ -9,6 +9,7 @@
 namespace fcdem {
 
 static_assert(sizeof(SimParams) == 104, "SimParams must keep the reference layout");
+static_assert(sizeof(fcdemRigidBody) == 40, "fcdemRigidBody keeps i3d::Rbody<float>'s fields");
 static_assert(offsetof(SimParams, colliderRadius) == 12, "layout");
 static_assert(offsetof(SimParams, gravity) == 16, "layout");
 static_assert(offsetof(SimParams, globalDamping) == 28, "layout");

@@ -307,6 +307,23 @@ def um_integrate_system(pos, vel, dt: float, n: int, dmap: DistanceMap | None) -
     lib.fcdemUM_integrateSystem(_p(pos), _p(vel), dt, n, dmap.handle if dmap else None)
 
 
+class RigidBody(C.Structure):
+    """fcdemRigidBody: i3d::Rbody<float>'s fields (cuda_addon/rbody.hpp)."""
+    _fields_ = [("numParticles", C.c_int), ("indices", C.c_int * 3), ("com", C.c_float * 3),
+                ("vel", C.c_float * 3)]
+
+
+lib.fcdemUM_integrateRigidBodies.argtypes = [C.c_void_p, C.c_uint, C.c_void_p, C.c_uint,
+                                             C.c_float]
+lib.fcdemUM_integrateRigidBodies.restype = None
+
+
+def um_integrate_rigid_bodies(bodies: torch.Tensor, num_bodies: int, pos, n: int,
+                              dt: float) -> None:
+    """bodies: a device byte tensor holding num_bodies RigidBody records."""
+    lib.fcdemUM_integrateRigidBodies(_p(bodies), num_bodies, _p(pos), n, dt)
+
+
 def um_eval_forces(new_vel, force, sorted_pos, sorted_vel, index, cell_start, cell_end,
                    n: int, num_cells: int) -> None:
     lib.fcdemUM_evalForces(_p(new_vel), _p(force), _p(sorted_pos), _p(sorted_vel), _p(index),

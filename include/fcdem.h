@@ -317,6 +317,25 @@ void fcdemUM_reorderDataAndFindCellStart(uint *cellStart, uint *cellEnd, float *
                                          uint *gridParticleIndex, float *oldPos, float *oldVel,
                                          uint numParticles, uint numCells);
 
+/* A rigid particle cluster, the fields of i3d::Rbody<float>
+ * (cuda_addon/rbody.hpp:10-22) in their order: member count, up to three
+ * member particle indices, centre of mass, velocity. */
+typedef struct fcdemRigidBody {
+  int numParticles;
+  int indices[3];
+  float com[3];
+  float vel[3];
+} fcdemRigidBody;
+
+/* particledem_um.cu:640-718 (d_integrateRigidBody): per body (device
+ * array), v += g dt, v *= globalDamping; com.z += v.z dt and vel.z = v.z are
+ * stored (the reference stores only z); each member particle's position
+ * moves by v dt (w = 1).  Members are the body's own indices (the reference
+ * hard-codes particles 0..2 for body 0 and 3..5 for the others, which is the
+ * same for its two three-particle bodies). */
+void fcdemUM_integrateRigidBodies(fcdemRigidBody *bodies, uint numBodies, float *pos,
+                                  uint numParticles, float deltaTime);
+
 /* ---------------------------------------------------------------------- */
 /* Neural signed-distance field of an obstacle (no counterpart in the
  * reference).  A small MLP -- inputs (x, y, z) normalised as
