@@ -654,6 +654,18 @@ def run_ours(args):
     # cell tables written once per call
     stage_bytes = {"integrate_hash": 72 * n, "sort": 88 * n + 8 * ncell, "fill": 8 * ncell,
                    "collide": 72 * n + 8 * occupied}
+    # the whole step: 228 N + 16 C algorithmic bytes (integrate 64 N, calcHash
+    # 24 N, sort 16 N, reorder 72 N + 8 C, collide 52 N + 8 C)
+    step_bytes = 228 * n + 16 * ncell
+    first = phases[0]["ms_per_step"] if phases else el_ms / args.steps
+    step_roofline = {"algorithmic_bytes": step_bytes,
+                     "job": {"ms_per_step": el_ms / args.steps,
+                             "achieved_gbs": step_bytes / (el_ms / args.steps / 1e3) / 1e9},
+                     "first_chunk": {"steps": phases[0]["steps"] if phases else None,
+                                     "ms_per_step": first,
+                                     "achieved_gbs": step_bytes / (first / 1e3) / 1e9}}
+    for v in (step_roofline["job"], step_roofline["first_chunk"]):
+        v["frac"] = v["achieved_gbs"] / peak
     stage_roofline = {}
     for k, b in stage_bytes.items():
         if stage_ms.get(k):
@@ -728,6 +740,7 @@ def run_ours(args):
                          "avg_launch_ms": stage_ms[dominant]},
             "stage_ms": stage_ms,
             "stage_roofline": stage_roofline,
+            "step_roofline": step_roofline,
             "phases": phases,
             "final_cells": final_cells,
             "batched": batched,
