@@ -164,6 +164,7 @@ __device__ __forceinline__ CellCull makeCull(float3 p, int3 g, float R, const Si
 // [q * kQueueStride + t]).
 constexpr int kQueueLen = 16;
 constexpr int kQueueStride = 128;
+constexpr int kStageLen = 128;  // staged partner positions per warp (collide row windows)
 
 // The 27-cell loop with cell tables and positions read from global memory,
 // in two phases.  The scan over candidates only tests the squared distance
@@ -179,7 +180,8 @@ template <bool kRadiusFromW, bool kPrefix>
 __device__ __forceinline__ float3 neighbourForceGlobal(
     unsigned i, unsigned n, float3 pos, float3 vel, float ri, int3 g, bool cull,
     const float4 *__restrict__ sortedPos, const float4 *__restrict__ sortedVel,
-    const CellRanges &cells, const SimParams &P, unsigned *qj, unsigned char *qc) {
+    const CellRanges &cells, const SimParams &P, unsigned *qj, unsigned char *qc,
+    float4 *stage = nullptr) {
   const float cdMono = ri + P.particleRadius;
   const float cdMonoHi2 = rejectBound(cdMono);
   // largest contact distance: r_i + particleRadius (in the radius-from-w
@@ -216,11 +218,12 @@ __device__ __forceinline__ float3 neighbourForceGlobal(
     }
     qn = 0;
   };
-  // queue a near partner j of neighbour cell `cell` (0..26)
-  auto scanRange = [&](unsigned a, unsigned b, int cellA, unsigned m1, unsigned m2) {
+  // queue a near partner j of neighbour cell `cell` (0..26); load(j) gives
+  // the position of sorted particle j (global or the warp's staged copy)
+  auto scanRange = [&](unsigned a, unsigned b, int cellA, unsigned m1, unsigned m2, auto load) {
     // cells cellA, cellA+1, cellA+2 hold [a, m1), [m1, m2), [m2, b)
     for (unsigned j = a; j < b; j++) {
-      float4 q4 = ldg4(sortedPos + j);
+      float4 q4 = load(j);
       float3 rel = make_float3(q4.x - pos.x, q4.y - pos.y, q4.z - pos.z);
       float d2 = pairDist2(rel);
       float hi2 = kRadiusFromW ? rejectBound(ri + q4.w) : cdMonoHi2;
@@ -232,26 +235,53 @@ __device__ __forceinline__ float3 neighbourForceGlobal(
       }
     }
   };
+  auto loadGlobal = [&](unsigned j) { return ldg4(sortedPos + j); };
+  const unsigned lane = threadIdx.x & 31u;
 #pragma unroll 1
   for (int row = 0; row < 9; row++) {
     const int z = row / 3 - 1, y = row % 3 - 1;
     const float rowD2 = CellCull::pick(z, cc.zl, cc.zh) + CellCull::pick(y, cc.yl, cc.yh);
-    if (rowD2 > cullR2) continue;
+    const bool rowLive = rowD2 <= cullR2;
     const bool useL = rowD2 + CellCull::pick(-1, cc.xl, cc.xh) <= cullR2;
     const bool useR = rowD2 + CellCull::pick(1, cc.xl, cc.xh) <= cullR2;
     if (kPrefix && !mortonOrder(P)) {
       const unsigned gxm = P.gridSize[0] - 1u;
       const unsigned xm = (unsigned)(g.x) & gxm;
-      if (xm >= 1u && xm < gxm) {
-        // no x wrap: the row's three cells are consecutive hashes, one range
+      const bool merged = xm >= 1u && xm < gxm;
+      // no x wrap: the row's three cells are consecutive hashes, one range
+      unsigned a = 0, b = 0, o1 = 0, o2 = 0;
+      if (merged && rowLive) {
         const unsigned h0 = gridHash(g.x - 1, g.y + y, g.z + z, P);
-        const unsigned o0 = __ldg(cells.off + h0), o1 = __ldg(cells.off + h0 + 1);
-        const unsigned o2 = __ldg(cells.off + h0 + 2), o3 = __ldg(cells.off + h0 + 3);
-        const unsigned a = useL ? o0 : o1, b = min(useR ? o3 : o2, n);
-        scanRange(a, b, row * 3, o1, o2);
-        continue;
+        const unsigned o0 = __ldg(cells.off + h0);
+        o1 = __ldg(cells.off + h0 + 1);
+        o2 = __ldg(cells.off + h0 + 2);
+        const unsigned o3 = __ldg(cells.off + h0 + 3);
+        a = useL ? o0 : o1;
+        b = min(useR ? o3 : o2, n);
       }
+      if (stage) {
+        // The lanes of a warp are consecutive sorted particles, mostly in
+        // one grid row: their ranges of this neighbour row overlap.  The
+        // warp copies the union into shared memory with coalesced loads and
+        // every lane scans its own range from there.
+        const unsigned am = __activemask();
+        const unsigned lo = __reduce_min_sync(am, a < b ? a : 0xffffffffu);
+        const unsigned hi = __reduce_max_sync(am, a < b ? b : 0u);
+        if (lo < hi && hi - lo <= (unsigned)kStageLen) {
+          const unsigned rank = __popc(am & ((1u << lane) - 1u)), lanes = __popc(am);
+          for (unsigned t = rank; t < hi - lo; t += lanes) stage[t] = ldg4(sortedPos + lo + t);
+          __syncwarp(am);
+          scanRange(a, b, row * 3, o1, o2, [&](unsigned j) { return stage[j - lo]; });
+          __syncwarp(am);  // the copy is reused by the next row
+        } else if (merged) {
+          scanRange(a, b, row * 3, o1, o2, loadGlobal);
+        }
+      } else if (merged) {
+        scanRange(a, b, row * 3, o1, o2, loadGlobal);
+      }
+      if (merged) continue;
     }
+    if (!rowLive) continue;
     unsigned h[3], start[3], end[3];
 #pragma unroll
     for (int x = 0; x < 3; x++) {
@@ -373,6 +403,7 @@ kCollideGlobal(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos
                CrowdList crowd, unsigned *status) {
   __shared__ unsigned qj[kQueueLen * kQueueStride];
   __shared__ unsigned char qc[kQueueLen * kQueueStride];
+  __shared__ float4 sStage[4][kStageLen];
   const SimParams &P = kp.p;
   unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -399,7 +430,7 @@ kCollideGlobal(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos
   }
   float3 force = neighbourForceGlobal<kRadiusFromW, kPrefix>(
       i, n, pos, vel, ri, g, cull, sortedPos, sortedVel, cells, P, qj + threadIdx.x,
-      qc + threadIdx.x);
+      qc + threadIdx.x, kPrefix ? sStage[threadIdx.x >> 5] : nullptr);
   finishParticle<kMode, kCollider, kForceOut>(i, n, pos, vel, p4, ri, force, index, newVel,
                                               out, P);
 }
@@ -805,6 +836,7 @@ kCollideBatch(const BatchScene *__restrict__ scenes, const unsigned *__restrict_
               const unsigned *__restrict__ off, unsigned n, CollideOut out, unsigned *status) {
   __shared__ unsigned qj[kQueueLen * kQueueStride];
   __shared__ unsigned char qc[kQueueLen * kQueueStride];
+  __shared__ float4 sStage[4][kStageLen];
   unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const BatchScene &S = scenes[__ldg(sceneOf + i)];
@@ -823,7 +855,8 @@ kCollideBatch(const BatchScene *__restrict__ scenes, const unsigned *__restrict_
   cells.off = off + S.cellBase;
   float3 force = neighbourForceGlobal<kRadiusFromW, true>(i, n, pos, vel, ri, g, cull,
                                                           sortedPos, sortedVel, cells, P,
-                                                          qj + threadIdx.x, qc + threadIdx.x);
+                                                          qj + threadIdx.x, qc + threadIdx.x,
+                                                          sStage[threadIdx.x >> 5]);
   // collider sphere (particles_kernel.cu:288)
   {
     float3 rel = make_float3(P.colliderPos[0] - pos.x, P.colliderPos[1] - pos.y,
