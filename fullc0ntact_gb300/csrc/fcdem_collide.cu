@@ -334,7 +334,7 @@ __device__ __forceinline__ float3 neighbourForceGlobal(
 // partner sequence: every partner load is one broadcast, no lane diverges
 // in its loop bounds, and each lane still sums its own terms cell by cell in
 // ascending partner order -- the reference's arithmetic.
-constexpr unsigned kCrowdLimit = 1024;
+constexpr unsigned kCrowdLimit = 512;
 constexpr int kCrowdWarps = 8;
 
 struct CrowdList {
@@ -428,9 +428,11 @@ kCollideGlobal(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos
     atomicOr(status, (unsigned)kStatusRadiusBound);
     cull = false;
   }
-  float3 force = neighbourForceGlobal<kRadiusFromW, kPrefix>(
-      i, n, pos, vel, ri, g, cull, sortedPos, sortedVel, cells, P, qj + threadIdx.x,
-      qc + threadIdx.x, kPrefix ? sStage[threadIdx.x >> 5] : nullptr);
+  float3 force = make_float3(0.0f, 0.0f, 0.0f);
+  if (!inertPos(pos))  // an inert particle's force is +0.0 (inertPos)
+    force = neighbourForceGlobal<kRadiusFromW, kPrefix>(
+        i, n, pos, vel, ri, g, cull, sortedPos, sortedVel, cells, P, qj + threadIdx.x,
+        qc + threadIdx.x, kPrefix ? sStage[threadIdx.x >> 5] : nullptr);
   finishParticle<kMode, kCollider, kForceOut>(i, n, pos, vel, p4, ri, force, index, newVel,
                                               out, P);
 }
@@ -475,6 +477,7 @@ kCollideCrowd(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
     const int gx = __shfl_sync(0xffffffffu, g.x, 0), gy = __shfl_sync(0xffffffffu, g.y, 0),
               gz = __shfl_sync(0xffffffffu, g.z, 0);
     valid = valid && gridHash(g.x, g.y, g.z, P) == gridHash(gx, gy, gz, P);
+    const bool scan = valid && !inertPos(pos);  // an inert member's force is +0.0
     bool lcull = cull;
     if (valid && kRadiusFromW && !(ri <= P.particleRadius)) {
       atomicOr(status, (unsigned)kStatusRadiusBound);
@@ -490,7 +493,7 @@ kCollideCrowd(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
       const int z = c27 / 9 - 1, y = (c27 / 3) % 3 - 1, x = c27 % 3 - 1;
       const float boxD2 = CellCull::pick(z, cc.zl, cc.zh) + CellCull::pick(y, cc.yl, cc.yh) +
                           CellCull::pick(x, cc.xl, cc.xh);
-      if (__all_sync(0xffffffffu, !valid || boxD2 > cullR2)) continue;
+      if (__all_sync(0xffffffffu, !scan || boxD2 > cullR2)) continue;
       unsigned a, b;
       cellRange<kPrefix>(gridHash(gx + x, gy + y, gz + z, P), cells, n, a, b);
       if (a >= b) continue;
@@ -503,6 +506,9 @@ kCollideCrowd(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
 #pragma unroll 1
       for (unsigned j0 = a; j0 < b; j0 += 32) {
         const unsigned cnt = min(32u, b - j0);
+        // partners of this chunk that are not inert; a chunk of inert
+        // partners only (the cells where NaN particles gather) adds nothing
+        const unsigned live = __ballot_sync(0xffffffffu, lane < cnt && !inertPos(nP));
         __syncwarp();  // the previous chunk is no longer read
         cPos[lane] = nP;
         cVel[lane] = nV;
@@ -511,6 +517,7 @@ kCollideCrowd(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
           nP = ldg4(sortedPos + jn);
           nV = ldg4(sortedVel + jn);
         }
+        if (live == 0u) continue;
         __syncwarp();
         // scan: squared-distance test, near partners queued in order
         int qn = 0;
@@ -520,7 +527,7 @@ kCollideCrowd(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
           const float3 rel = make_float3(q4.x - pos.x, q4.y - pos.y, q4.z - pos.z);
           const float d2 = pairDist2(rel);
           const float hi2 = kRadiusFromW ? rejectBound(ri + q4.w) : cdMonoHi2;
-          if (valid && d2 < hi2 && j0 + t != i) {
+          if (scan && d2 < hi2 && j0 + t != i) {
             q[qn * 32] = (unsigned char)t;
             ++qn;
           }
@@ -836,7 +843,6 @@ kCollideBatch(const BatchScene *__restrict__ scenes, const unsigned *__restrict_
               const unsigned *__restrict__ off, unsigned n, CollideOut out, unsigned *status) {
   __shared__ unsigned qj[kQueueLen * kQueueStride];
   __shared__ unsigned char qc[kQueueLen * kQueueStride];
-  __shared__ float4 sStage[4][kStageLen];
   unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const BatchScene &S = scenes[__ldg(sceneOf + i)];
@@ -853,10 +859,11 @@ kCollideBatch(const BatchScene *__restrict__ scenes, const unsigned *__restrict_
   }
   CellRanges cells;
   cells.off = off + S.cellBase;
-  float3 force = neighbourForceGlobal<kRadiusFromW, true>(i, n, pos, vel, ri, g, cull,
-                                                          sortedPos, sortedVel, cells, P,
-                                                          qj + threadIdx.x, qc + threadIdx.x,
-                                                          sStage[threadIdx.x >> 5]);
+  float3 force = make_float3(0.0f, 0.0f, 0.0f);
+  if (!inertPos(pos))
+    force = neighbourForceGlobal<kRadiusFromW, true>(i, n, pos, vel, ri, g, cull, sortedPos,
+                                                     sortedVel, cells, P, qj + threadIdx.x,
+                                                     qc + threadIdx.x);
   // collider sphere (particles_kernel.cu:288)
   {
     float3 rel = make_float3(P.colliderPos[0] - pos.x, P.colliderPos[1] - pos.y,

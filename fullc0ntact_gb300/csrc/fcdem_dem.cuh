@@ -134,6 +134,22 @@ __device__ __forceinline__ float pairDist2(float3 rel) {
 
 __device__ __forceinline__ float pairDist(float3 rel) { return sqrtf(pairDist2(rel)); }
 
+// A particle with a NaN or infinite coordinate takes part in no pair term:
+// every squared distance to it is NaN or +inf, and neither passes the
+// contact tests (`d2 < bound`, `dist < cd`, false for NaN and for +inf
+// against a finite bound; an infinite bound needs an infinite radius and
+// +inf < +inf is false too).  Its force is therefore +0.0, its partners get
+// nothing from it, and skipping it leaves every sum unchanged.  Such
+// particles arise in the reference's own arithmetic: two spheres of equal
+// radius clamped into the same box corner coincide, dist = 0, and the
+// normal rel / dist is NaN.
+__device__ __forceinline__ bool inertPos(float3 p) {
+  return !(isfinite(p.x) && isfinite(p.y) && isfinite(p.z));
+}
+__device__ __forceinline__ bool inertPos(float4 p) {
+  return !(isfinite(p.x) && isfinite(p.y) && isfinite(p.z));
+}
+
 // Squared-distance bound for the contact test: d2 >= rejectBound(cd) implies
 // sqrtf(d2) >= cd, so such a pair cannot pass `dist < cd` and is skipped
 // without the (multi-instruction) IEEE square root.  Proof: the computed

@@ -186,7 +186,7 @@ void fcdemSetCellCulling(int on);
  * that. */
 void fcdemSetCrowdPath(int on);
 /* Neighbourhood size above which the crowded path takes a particle
- * (0: the default, 1024). */
+ * (0: the default, 512). */
 void fcdemSetCrowdLimit(uint limit);
 
 /* Cell-key order (no counterpart in the reference; default 0, the

@@ -134,3 +134,65 @@ def test_crowd_path_is_exact(kind, pipeline):
     b = _run_crowd(sc, False, 3, pipeline)
     for x, y in zip(a, b):
         np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
+
+
+def _inert_scene():
+    """Packed polydisperse scene with particles that take part in no pair
+    term: 3,000 with NaN positions (they share one cell, a crowded
+    neighbourhood), 300 with one NaN coordinate, and 40 spheres of equal
+    radius at one point (coincident: dist = 0, their normals are NaN)."""
+    from fullc0ntact_gb300 import scenes
+    sc = scenes.packed_scene(100_000, grid=128)
+    rng = np.random.default_rng(31)
+    picks = rng.permutation(sc["pos"].shape[0])
+    sc["pos"][picks[:3000], :3] = np.float32(np.nan)
+    for k, idx in enumerate(np.array_split(picks[3000:3300], 3)):
+        sc["pos"][idx, k] = np.float32(np.nan)
+    same = picks[3300:3340]
+    sc["pos"][same, :3] = np.float32(0.25)
+    sc["pos"][same, 3] = np.float32(sc["params"].particleRadius)
+    sc["vel"][same, :3] = np.float32(0.0)  # still coincident after the integrate
+    return sc
+
+
+def test_inert_particles_match_oracle():
+    """Particles with a NaN coordinate are skipped by collide (their force is
+    +0.0 and they give their partners nothing); the oracle walks them like
+    every other particle.  One update through the reference-named stages:
+    hashes and order bit for bit, new velocities within the 1e-5 bar with
+    NaN exactly where the oracle has NaN."""
+    from fullc0ntact_gb300 import dem
+    from oracle import oracle as O
+    from fcdem_testutil import REL_TOL, force_floor, oracle_params, rel_err_vec
+    sc = _inert_scene()
+    ds = dem.DeviceScene(sc)
+    ds.stages()
+    dem.check("stages with inert particles")
+    st = O.step_stages(oracle_params(bytes(sc["params"])), sc["pos"], sc["vel"], sc["dt"],
+                       radius_from_w=True)
+    np.testing.assert_array_equal(ds.hash.cpu().numpy().view(np.uint32), st["hash_sorted"])
+    np.testing.assert_array_equal(ds.index.cpu().numpy().view(np.uint32), st["index_sorted"])
+    out = ds.vel.cpu().numpy()
+    np.testing.assert_array_equal(np.isnan(out[:, :3]), np.isnan(st["newVel"][:, :3]))
+    assert int(np.isnan(out[:, 0]).sum()) >= 40  # the coincident spheres
+    # a particle with a NaN coordinate keeps its velocity (force +0.0)
+    inert = np.isnan(st["pos"][:, :3]).any(axis=1)
+    assert int(inert.sum()) == 3300
+    keep = st["vel_in"][inert, :3] + np.float32(0.0)
+    np.testing.assert_array_equal(out[inert, :3].view(np.uint32), keep.view(np.uint32))
+    f_ref = st["newVel"][:, :3].astype(np.float64) - st["vel_in"][:, :3]
+    f_gpu = out[:, :3].astype(np.float64) - st["vel_in"][:, :3]
+    assert rel_err_vec(out, st["newVel"], 1e-6).max() <= REL_TOL
+    assert rel_err_vec(f_gpu, f_ref, force_floor(f_ref)).max() <= REL_TOL
+
+
+@pytest.mark.parametrize("pipeline", [0, 1])
+def test_inert_particles_identical_on_every_path(pipeline):
+    """Five fused updates of the scene with inert particles: the crowded
+    kernel (which skips chunks of inert partners) and the per-thread kernel
+    give the same bits."""
+    sc = _inert_scene()
+    a = _run_crowd(sc, True, 5, pipeline)
+    b = _run_crowd(sc, False, 5, pipeline)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
