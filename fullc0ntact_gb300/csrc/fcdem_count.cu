@@ -312,13 +312,76 @@ kFixupGather(const unsigned *__restrict__ slotKey, const unsigned *__restrict__ 
 constexpr int kLargeThreads = 1024;
 constexpr int kLargeWarps = kLargeThreads / 32;
 constexpr int kLargeCtas = 152;
+constexpr int kBitmapSlots = 16;  // CTAs of kFixupLarge that own a bitmap
+
+// Words of one bitmap slot: a presence bit per particle index.
+__host__ __device__ inline size_t bitmapWords(unsigned n) { return (size_t)n / 32 + 1; }
 
 struct LargeSmem {
   unsigned bin[256];                  // running base of each digit
   unsigned total[256];                // a chunk's count of each digit
   unsigned part[8];                   // warp totals of the digit scan
   unsigned warpCnt[kLargeWarps][256]; // per-warp digit counts of a chunk
+  unsigned warpSum[kLargeWarps];      // bitmap path: popcount of each warp's run
+  unsigned lo, hi;                    // bitmap path: smallest / largest member index
 };
+
+// Bitmap rank of a large cell's members (the members' particle indices are
+// distinct): bit i of `bits` is set for member index i; pre[w] is the number
+// of set bits in words w0 .. w-1; the rank of member i among the cell's
+// members is pre[i / 32] + the set bits below i in its word.  Words w0..w1
+// (the members' index span) are cleared, filled, counted and scanned: the
+// work grows with the span, not with the member count, so the caller takes
+// this path when the span is at most kBitmapSpan words per member.
+constexpr unsigned kBitmapSpan = 16;
+
+__device__ void bitmapRanks(const unsigned *slotOrig, unsigned a, unsigned c, unsigned n,
+                            unsigned w0, unsigned w1, unsigned *bits, unsigned *pre,
+                            LargeSmem &sm) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (unsigned w = w0 + tid; w <= w1; w += kLargeThreads) bits[w] = 0u;
+  __syncthreads();
+  for (unsigned t = tid; t < c; t += kLargeThreads) {
+    const unsigned me = slotOrig[a + t];
+    if (me < n) atomicOr(bits + (me >> 5), 1u << (me & 31u));
+  }
+  __syncthreads();
+  // each warp owns a contiguous run of words: its total, then the scan
+  const unsigned span = w1 - w0 + 1u;
+  const unsigned run = ((span + kLargeWarps - 1u) / kLargeWarps + 31u) & ~31u;
+  const unsigned ws = w0 + (unsigned)warp * run;
+  const unsigned we = min(ws + run, w1 + 1u);
+  unsigned sum = 0;
+  for (unsigned w = ws + lane; w < we; w += 32) sum += __popc(bits[w]);
+  sum = __reduce_add_sync(0xffffffffu, sum);
+  if (lane == 0) sm.warpSum[warp] = sum;
+  __syncthreads();
+  if (warp == 0) {
+    const unsigned v = sm.warpSum[lane];
+    unsigned x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    sm.warpSum[lane] = x - v;
+  }
+  __syncthreads();
+  unsigned carry = sm.warpSum[warp];
+  for (unsigned base = ws; base < we; base += 32) {
+    const unsigned w = base + lane;
+    const unsigned v = w < we ? __popc(bits[w]) : 0u;
+    unsigned x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (w < we) pre[w] = carry + x - v;
+    carry += __shfl_sync(0xffffffffu, x, 31);
+  }
+  __syncthreads();
+}
 
 // One stable pass of a block-wide LSD radix sort: src[0..c) -> dst[0..c)
 // by the 8-bit digit at bit `shift`.  Chunks of kLargeThreads entries go in
@@ -390,15 +453,60 @@ kFixupLarge(unsigned *__restrict__ slotOrig, unsigned *__restrict__ slotPrev,
             unsigned largeCap, unsigned *__restrict__ hashOut, unsigned *__restrict__ indexOut,
             float4 *__restrict__ sortedPos, float4 *__restrict__ sortedVel,
             const float4 *__restrict__ prevPos, const float4 *__restrict__ prevVel, unsigned n,
-            int idBits) {
+            int idBits, unsigned *__restrict__ bitmaps) {
   __shared__ LargeSmem sm;
   const unsigned count = min(large[0], largeCap);
   const int tid = threadIdx.x;
+  const size_t words = bitmapWords(n);
+  unsigned *bits = blockIdx.x < (unsigned)kBitmapSlots && bitmaps
+                       ? bitmaps + (size_t)blockIdx.x * 2u * words
+                       : nullptr;
   for (unsigned k = blockIdx.x; k < count; k += gridDim.x) {
     const unsigned h = large[1 + k];
     const unsigned a = off[h], b = off[h + 1];
     if (b > n || a >= b) continue;  // cannot happen for a listed cell
     const unsigned c = b - a;
+    if (bits) {
+      // the members' index span decides between the bitmap and the sort
+      if (tid == 0) {
+        sm.lo = 0xffffffffu;
+        sm.hi = 0u;
+      }
+      __syncthreads();
+      unsigned lo = 0xffffffffu, hi = 0u;
+      for (unsigned t = tid; t < c; t += kLargeThreads) {
+        const unsigned me = slotOrig[a + t];
+        if (me < n) {
+          lo = min(lo, me);
+          hi = max(hi, me);
+        }
+      }
+      lo = __reduce_min_sync(0xffffffffu, lo);
+      hi = __reduce_max_sync(0xffffffffu, hi);
+      if ((tid & 31) == 0) {
+        atomicMin(&sm.lo, lo);
+        atomicMax(&sm.hi, hi);
+      }
+      __syncthreads();
+      const unsigned mlo = sm.lo, mhi = sm.hi;
+      const unsigned w0 = mlo >> 5, w1 = mhi >> 5;
+      if (mlo <= mhi && w1 - w0 + 1u <= kBitmapSpan * c) {
+        unsigned *pre = bits + words;
+        bitmapRanks(slotOrig, a, c, n, w0, w1, bits, pre, sm);
+        for (unsigned t = tid; t < c; t += kLargeThreads) {
+          const unsigned me = slotOrig[a + t], prev = slotPrev[a + t];
+          if (me >= n || prev >= n) continue;  // unfilled slot (reported by the scatter)
+          const unsigned wd = me >> 5;
+          const unsigned dst = a + pre[wd] + __popc(bits[wd] & ((1u << (me & 31u)) - 1u));
+          hashOut[dst] = h;
+          indexOut[dst] = me;
+          sortedPos[dst] = ldg4(prevPos + prev);
+          sortedVel[dst] = ldg4(prevVel + prev);
+        }
+        __syncthreads();  // the bitmap is reused by the next cell
+        continue;
+      }
+    }
     unsigned long long *A = reinterpret_cast<unsigned long long *>(sortedPos + a);
     unsigned long long *B = A + c;
     for (unsigned t = tid; t < c; t += kLargeThreads)
@@ -537,7 +645,8 @@ bool countBuffersIn(void *&buf, size_t &bytes, unsigned &cells, unsigned n, unsi
   const unsigned largeCap = largeCapacity(n);
   const unsigned tileBlocks = (tiles + kTileBlock - 1) / kTileBlock;
   const size_t need = 2 * al(m * 4) + 4 * al((size_t)n * 4) + 2 * al((size_t)(tiles + 1) * 4) +
-                      al(((size_t)largeCap + 1) * 4) + al((size_t)tileBlocks * 4);
+                      al(((size_t)largeCap + 1) * 4) + al((size_t)tileBlocks * 4) +
+                      al((size_t)kBitmapSlots * 2 * bitmapWords(n) * 4);
   if (buf == nullptr || bytes < need || cells != numCells) {
     if (!cudaOk(cudaDeviceSynchronize())) return false;
     if (buf) cudaFree(buf);
@@ -577,6 +686,8 @@ bool countBuffersIn(void *&buf, size_t &bytes, unsigned &cells, unsigned n, unsi
   b.largeCap = largeCap;
   p += al(((size_t)largeCap + 1) * 4);
   b.tileBlockSum = (unsigned *)p;
+  p += al((size_t)tileBlocks * 4);
+  b.bitmaps = (unsigned *)p;  // cleared where used (kFixupLarge)
   b.scanTiles = tiles;
   return true;
 }
@@ -640,7 +751,8 @@ bool countPipelineSort(Context &c, const CountBuffers &b, const unsigned *origOf
   const unsigned largeCtas = b.largeCap < (unsigned)kLargeCtas ? b.largeCap : kLargeCtas;
   kFixupLarge<<<largeCtas, kLargeThreads, 0, st>>>(b.slotIdx, b.slotPrev, b.off, b.large,
                                                    b.largeCap, hash, index, sortedPos,
-                                                   sortedVel, prevPos, prevVel, n, keyBits(n));
+                                                   sortedVel, prevPos, prevVel, n, keyBits(n),
+                                                   b.bitmaps);
   return launchOk();
 }
 

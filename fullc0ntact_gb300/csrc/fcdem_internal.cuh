@@ -164,6 +164,7 @@ struct CountBuffers {
   unsigned *tileCnt, *tileOff;  // per 4096-cell tile: counts and their prefix
   unsigned *large;              // [0] = count, [1..largeCap] = cells too full for the re-rank
   unsigned *tileBlockSum;       // per 1024 tiles: their total (many-tile scans)
+  unsigned *bitmaps;            // kFixupLarge: per-CTA bitmap + word prefix of particle indices
   unsigned scanTiles, largeCap;
 };
 bool countPipelineBegin(Context &c, float4 *pos, float4 *vel, float dt, unsigned *hash,

@@ -137,17 +137,22 @@ def test_counting_pipeline_on_packed_scene_and_crowded_cells():
             np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
 
 
-@pytest.mark.parametrize("n,grid", [(6000, 8), (100_000, 128)])
-def test_counting_pipeline_cells_above_rerank_limit(n, grid):
-    """Cells holding more than the per-slot re-rank handles (1,024) go to the
-    block radix sort of their members; the result stays identical to the
-    staged radix-sort path.  n = 100,000 needs three 8-bit passes over the
-    particle index, n = 6,000 two."""
+@pytest.mark.parametrize("n,kind", [(6000, "box8"), (100_000, "packed"), (1_000_000, "box128")])
+def test_counting_pipeline_cells_above_rerank_limit(n, kind):
+    """Cells holding more than the per-slot re-rank handles (1,024) are
+    ranked by particle index in one CTA each: with a bitmap of the members'
+    indices when their span is at most 16 words per member, else with a
+    block radix sort (n = 100,000 needs three 8-bit passes, n = 6,000 two).
+    At n = 1,000,000 the 3,000-member cell takes the bitmap and the 1,500-
+    and 1,025-member cells the sort; at the smaller n every cell takes the
+    bitmap.  The result stays identical to the staged radix-sort path."""
     from fullc0ntact_gb300 import dem, scenes
-    if grid == 8:
+    if kind == "box8":
         sc = scenes.random_box(n, grid=(8, 8, 8), radius=0.02, cell=0.25, seed=11)
+    elif kind == "box128":
+        sc = scenes.random_box(n, grid=(128, 128, 128), radius=1.0 / 128.0, seed=13)
     else:
-        sc = scenes.packed_scene(n, grid=grid)
+        sc = scenes.packed_scene(n, grid=128)
     rng = np.random.default_rng(5)
     cell = float(sc["params"].cellSize[0])
     origin = np.array([sc["params"].worldOrigin[k] for k in range(3)], np.float32)
