@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--chunk", type=int, default=50,
                     help="steps between the events that report step time along the job")
     ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--advance", type=int, default=0,
+                    help="start the timed job from the packed state advanced by this many "
+                         "untimed steps (to measure or profile a later phase of the job)")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=4194304, help="particles (default: the full workload)")
     ap.add_argument("--cpu-steps", type=int, default=20, help="CPU-baseline sample steps")
@@ -579,11 +582,15 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize()
 
-    # The job is K steps from the packed initial state; every measured phase
-    # (timed, stage attribution, end to end) starts from that state, so each
-    # covers the same steps.  Late in the job the pile, held up only by the
-    # soft contact springs (spring 0.5), collapses into a few very crowded
-    # cells whose collide cost grows with the square of their occupancy.
+    # The job is K steps from the packed initial state (or from that state
+    # advanced by --advance untimed steps); every measured phase (timed, stage
+    # attribution, end to end) starts from it, so each covers the same steps.
+    # Along the job the spheres settle into dense lower layers, and particles
+    # with NaN coordinates (coincident equal spheres clamped into a box
+    # corner, as in the reference's arithmetic) gather in a few cells.
+    if args.advance > 0:
+        ds.update(args.advance)
+        dem.check("advance")
     pos0, vel0 = ds.pos.clone(), ds.vel.clone()
 
     def reset():
@@ -604,11 +611,13 @@ def run_ours(args):
     evs = [torch.cuda.Event(enable_timing=True) for _ in bounds]
     barrier()
     l0 = lib.fcdemGetLaunchCount()
+    torch.cuda.nvtx.range_push("fcdem_timed")  # profilers can select this range
     evs[0].record()
     for k in range(1, len(bounds)):
         ds.update(bounds[k] - bounds[k - 1])
         evs[k].record()
     barrier()
+    torch.cuda.nvtx.range_pop()
     launches = int(lib.fcdemGetLaunchCount() - l0)
     el_ms = max_over_ranks(evs[0].elapsed_time(evs[-1]), f"cuda:{dev}")
     dem.check("timed updates")
@@ -723,7 +732,8 @@ def run_ours(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": el_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded packing)",
-            "config": {"workload": f"{WORKLOAD}, {args.steps}-step job from the packed state",
+            "config": {"workload": f"{WORKLOAD}, {args.steps}-step job from the packed state"
+                                   + (f" advanced by {args.advance} steps" if args.advance else ""),
                        "n": n, "grid": 256, "cells": ncell,
                        "occupied_cells": occupied, "step": "fcdemUpdate (fused update)",
                        "sort_config": sort_cfg, "cell_order": args.cell_order,
