@@ -28,6 +28,7 @@ constexpr unsigned kFlagAgg = 1u << 30;
 constexpr unsigned kFlagPrefix = 2u << 30;
 constexpr unsigned kValueMask = (1u << 30) - 1u;
 constexpr unsigned kSpinLimit = 1u << 22;
+constexpr int kLookWindow = 8;  // look-back tiles read per round
 
 
 __device__ __forceinline__ unsigned lanemaskLt() {
@@ -85,37 +86,57 @@ __device__ __forceinline__ unsigned blockExclusiveScan(unsigned v, unsigned *war
 }
 
 // Histograms of all `passes` digits; checks that no key has bits at or above
-// `bits`.  hist must be zero on entry.
+// `bits`.  hist must be zero on entry.  Each warp counts into its own copy
+// of the histograms (shared-memory atomics of one warp only contend with its
+// own lanes); a digit that all lanes of the warp share (sorted or clustered
+// keys) is added once.  The copies are summed at the end.
+constexpr int kUpWarps = kThreads / 32;
+constexpr int kUpKeys = 4;
 __global__ void __launch_bounds__(kThreads)
 kUpsweep(const unsigned *__restrict__ keys, unsigned n, int passes, int bits,
          unsigned *__restrict__ hist, unsigned *__restrict__ status) {
-  __shared__ unsigned sh[kMaxPasses][kRadix];
-  for (int k = threadIdx.x; k < kMaxPasses * kRadix; k += kThreads)
-    (&sh[0][0])[k] = 0;
+  __shared__ unsigned sh[kUpWarps][kMaxPasses][kRadix];
+  for (int k = threadIdx.x; k < kUpWarps * kMaxPasses * kRadix; k += kThreads)
+    (&sh[0][0][0])[k] = 0;
   __syncthreads();
-  const unsigned lt = lanemaskLt();
-  const unsigned lane = threadIdx.x & 31;
+  const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   bool bad = false;
-  unsigned stride = gridDim.x * kThreads;
-  unsigned nRound = (n + 31u) & ~31u;
-  for (unsigned base = blockIdx.x * kThreads + (threadIdx.x & ~31u); base < nRound;
-       base += stride) {
-    unsigned i = base + lane;
-    bool valid = i < n;
-    unsigned k = valid ? __ldg(keys + i) : 0u;
-    if (valid && bits < 32 && (k >> bits) != 0u) bad = true;
-    unsigned active = __ballot_sync(0xffffffffu, valid);
-    for (int p = 0; p < passes; ++p) {
-      unsigned d = (k >> (p * kRadixBits)) & (kRadix - 1);
-      unsigned peers = digitPeers(d, active);
-      if (valid && (peers & lt) == 0u) atomicAdd(&sh[p][d], (unsigned)__popc(peers));
+  // kUpKeys keys per thread and round, their loads issued together
+  const unsigned stride = gridDim.x * kThreads;
+  const unsigned nRound = (n + 31u) & ~31u;
+  for (unsigned i0 = blockIdx.x * kThreads + threadIdx.x; i0 < nRound; i0 += kUpKeys * stride) {
+    unsigned k[kUpKeys];
+    bool valid[kUpKeys];
+#pragma unroll
+    for (int u = 0; u < kUpKeys; ++u) {
+      const unsigned i = i0 + u * stride;
+      valid[u] = i < n;
+      k[u] = valid[u] ? __ldg(keys + i) : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < kUpKeys; ++u) {
+      if (i0 + u * stride >= nRound) break;  // warp-uniform: nRound and stride are multiples of 32
+      if (valid[u] && bits < 32 && (k[u] >> bits) != 0u) bad = true;
+      const unsigned active = __ballot_sync(0xffffffffu, valid[u]);
+      for (int p = 0; p < passes; ++p) {
+        const unsigned d = (k[u] >> (p * kRadixBits)) & (kRadix - 1);
+        int same = 0;
+        __match_all_sync(0xffffffffu, valid[u] ? d : kRadix, &same);
+        if (same) {
+          if (lane == 0 && active) atomicAdd(&sh[warp][p][d], (unsigned)__popc(active));
+        } else if (valid[u]) {
+          atomicAdd(&sh[warp][p][d], 1u);
+        }
+      }
     }
   }
   if (bad) atomicOr(status, (unsigned)kStatusKeyRange);
   __syncthreads();
-  for (int p = 0; p < passes; ++p) {
-    unsigned c = sh[p][threadIdx.x];
-    if (c) atomicAdd(hist + p * kRadix + threadIdx.x, c);
+  for (int e = threadIdx.x; e < passes * kRadix; e += kThreads) {
+    unsigned c = 0;
+#pragma unroll
+    for (int w = 0; w < kUpWarps; ++w) c += (&sh[w][0][0])[e];
+    if (c) atomicAdd(hist + e, c);
   }
 }
 
@@ -202,22 +223,37 @@ kOnesweep(const unsigned *__restrict__ keysIn, const unsigned *__restrict__ vals
       stVolatile(row + b, kFlagPrefix | count);
     } else {
       stVolatile(row + b, kFlagAgg | count);
+      // Look back kLookWindow tiles per round: their words are loaded
+      // together (one latency for the window) and consumed nearest first,
+      // adding aggregates until an inclusive prefix; a tile that has not
+      // published yet ends the round, and the next round starts there.
       int t = (int)tile - 1;
       unsigned spins = 0;
-      while (t >= 0) {
-        unsigned w = ldVolatile(lookback + (size_t)t * kRadix + b);
-        unsigned flag = w & ~kValueMask;
-        if (flag == 0u) {
+      bool done = false;
+      while (!done) {
+        unsigned w[kLookWindow];
+#pragma unroll
+        for (int j = 0; j < kLookWindow; ++j)
+          w[j] = t - j >= 0 ? ldVolatile(lookback + (size_t)(t - j) * kRadix + b) : 0u;
+        int used = 0;
+#pragma unroll
+        for (int j = 0; j < kLookWindow; ++j) {
+          if (done || used < j) continue;  // stopped at an unpublished tile
+          const unsigned flag = w[j] & ~kValueMask;
+          if (flag == 0u) continue;
+          excl += w[j] & kValueMask;
+          used = j + 1;
+          if (flag == kFlagPrefix) done = true;
+        }
+        if (done) break;
+        t -= used;  // t >= 0: tile 0 publishes a prefix, so the walk stops there
+        if (used == 0) {
           if (++spins > kSpinLimit) {
             atomicOr(status, (unsigned)kStatusTimeout);
             break;
           }
           if (spins > 64) __nanosleep(64);
-          continue;
         }
-        excl += w & kValueMask;
-        if (flag == kFlagPrefix) break;
-        --t;
       }
       stVolatile(row + b, kFlagPrefix | ((excl + count) & kValueMask));
     }
