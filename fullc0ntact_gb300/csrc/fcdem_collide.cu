@@ -324,7 +324,7 @@ __device__ __forceinline__ float3 neighbourForceGlobal(
 
 // ---------------------------------------------------------------------------
 // Crowded neighbourhoods.  When a particle's 27 neighbour cells hold more
-// than kCrowdLimit particles (a collapsed pile), one thread walking them all
+// than kCrowdLimit particles (a dense pile), one thread walking them all
 // is a long serial loop and the few warps that hold such particles leave the
 // SMs idle.  kCollideGlobal then defers the particle: the members of its
 // cell are listed in groups of up to 32 consecutive sorted particles (the
