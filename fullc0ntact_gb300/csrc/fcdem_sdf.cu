@@ -517,7 +517,7 @@ __device__ __forceinline__ void sdfTileTeardown(SdfTileSmem<H, L> &sm) {
 // `shape` or -1); 128 threads, one point each, all threads of the CTA.
 // `phase` is the barrier parity, flipped per MMA chain.  Returns false (for
 // every thread) when an MMA chain did not complete in time.
-template <int H, int L>
+template <int H, int L, int kLdBatch = 1>
 __device__ __forceinline__ bool sdfTileForward(SdfTileSmem<H, L> &sm, const SdfView &net,
                                                float x0, float x1, float x2, int shape,
                                                unsigned &phase, float &dOut) {
@@ -570,23 +570,34 @@ __device__ __forceinline__ bool sdfTileForward(SdfTileSmem<H, L> &sm, const SdfV
     }
     tcFenceAfter();
     const bool last = (l == L - 1);
+    // kLdBatch column chunks of 16 are read from TMEM before one wait (more
+    // loads in flight, more registers: the standalone inference kernel uses
+    // 4, the fused culling kernels, which hold a particle's state, 1)
+    static_assert((H / 16) % kLdBatch == 0, "column chunks per batch");
 #pragma unroll 1
-    for (int c = 0; c < H / 16; ++c) {
-      float r[16];
-      tmemLoad16(sm.tmem + ((unsigned)(32 * warp) << 16) + (unsigned)(c * 16), r);
+    for (int c0 = 0; c0 < H / 16; c0 += kLdBatch) {
+      float r[kLdBatch][16];
+#pragma unroll
+      for (int q = 0; q < kLdBatch; ++q)
+        tmemLoad16(sm.tmem + ((unsigned)(32 * warp) << 16) + (unsigned)((c0 + q) * 16), r[q]);
       tmemWaitLoad();
 #pragma unroll
-      for (int u = 0; u < 16; ++u) r[u] = siluFast(r[u] + sm.b[l * H + c * 16 + u]);
-      if (last) {
+      for (int q = 0; q < kLdBatch; ++q) {
+        const int c = c0 + q;
 #pragma unroll
-        for (int u = 0; u < 16; ++u) y = fmaf(r[u], sm.wo[c * 16 + u], y);
-      } else {
+        for (int u = 0; u < 16; ++u) r[q][u] = siluFast(r[q][u] + sm.b[l * H + c * 16 + u]);
+        if (last) {
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          uint4 v = make_uint4(packBf16(r[8 * h], r[8 * h + 1]), packBf16(r[8 * h + 2], r[8 * h + 3]),
-                               packBf16(r[8 * h + 4], r[8 * h + 5]),
-                               packBf16(r[8 * h + 6], r[8 * h + 7]));
-          *reinterpret_cast<uint4 *>(sm.a + tileOffset(t, c * 16 + 8 * h, 128)) = v;
+          for (int u = 0; u < 16; ++u) y = fmaf(r[q][u], sm.wo[c * 16 + u], y);
+        } else {
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            uint4 v = make_uint4(packBf16(r[q][8 * h], r[q][8 * h + 1]),
+                                 packBf16(r[q][8 * h + 2], r[q][8 * h + 3]),
+                                 packBf16(r[q][8 * h + 4], r[q][8 * h + 5]),
+                                 packBf16(r[q][8 * h + 6], r[q][8 * h + 7]));
+            *reinterpret_cast<uint4 *>(sm.a + tileOffset(t, c * 16 + 8 * h, 128)) = v;
+          }
         }
       }
     }
@@ -614,7 +625,7 @@ kSdfInfer(SdfView net, const float4 *__restrict__ pts, const int *__restrict__ s
     const float4 q = valid ? __ldg(pts + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const int shape = (valid && shapes) ? __ldg(shapes + i) : -1;
     float d = 0.0f;
-    if (!sdfTileForward<H, L>(sm, net, (q.x - net.shift[0]) * net.scale[0],
+    if (!sdfTileForward<H, L, 4>(sm, net, (q.x - net.shift[0]) * net.scale[0],
                               (q.y - net.shift[1]) * net.scale[1],
                               (q.z - net.shift[2]) * net.scale[2], shape, phase, d)) {
       if (threadIdx.x == 0) atomicOr(status, (unsigned)kStatusTimeout);
