@@ -1,8 +1,12 @@
 """The FP32 force error against an FP64 evaluation of the same collide (the
 oracle's FP64 twin on the same sorted arrays), stated per workload: the
 packed polydisperse scene, the torus-fall scene's evalForces (force_
-output, no collider) and a scene with collapsed cells (the crowded-
-neighbourhood kernel).  The error is relative to max(|F|, median |F|)."""
+output, no collider), a scene with collapsed cells (the crowded-
+neighbourhood kernel), the largest kind of scene of the batched workload
+(65,536 spheres, radii U[1/512, 1/256], 25% packing) and a scene of the
+batched obstacle workload after 150 batched steps onto its rounded box (a
+batch gives each scene the bits of that scene alone).  The error is
+relative to max(|F|, median |F|)."""
 import numpy as np
 import pytest
 
@@ -25,12 +29,31 @@ def _collapsed(sc, counts, cells):
     return sc
 
 
-@pytest.mark.parametrize("kind", ["packed", "collapsed", "torus_um"])
+def _obstacle_pile(steps=150):
+    """A batched-obstacle scene after `steps` batched steps onto its obstacle
+    (the first rounded box of the obstacle set)."""
+    from fullc0ntact_gb300 import dem, scenes, sdf
+    obs = scenes.obstacle_set()
+    ob = next(o for o in obs if o["kind"] != "torus")
+    sc = scenes.obstacle_scene(120_000, ob, seed=7)
+    b = dem.Batch([sc])
+    b.set_obstacles(sdf.obstacle_maps([ob], 64), [0])
+    b.update(steps, graph=False)
+    dem.check("obstacle batch")
+    return dict(sc, pos=b.pos.cpu().numpy().copy(), vel=b.vel.cpu().numpy().copy())
+
+
+@pytest.mark.parametrize("kind", ["packed", "collapsed", "torus_um", "batch_scene",
+                                  "obstacle_pile"])
 def test_force_error_against_fp64(kind):
     from fullc0ntact_gb300 import dem, scenes
     from oracle import oracle as O
     if kind == "packed":
         sc = scenes.packed_scene(200_000, grid=128)
+    elif kind == "batch_scene":
+        sc = scenes.batch_scene(65_536, seed=17)
+    elif kind == "obstacle_pile":
+        sc = _obstacle_pile()
     elif kind == "collapsed":
         sc = _collapsed(scenes.packed_scene(100_000, grid=128), (2500, 700, 300),
                         ((5, 5, 5), (6, 5, 5), (9, 9, 9)))
