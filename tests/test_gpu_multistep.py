@@ -10,7 +10,9 @@ in a 256^3 grid, 500 steps, and a 100,000-sphere version of it):
 * one 500-step fcdemUpdate call (the state kept in sorted order between
   steps) ends in exactly the state of 500 single-step calls;
 * trajectories are chaotic, so a 100-step run is compared with the oracle's
-  by total kinetic and potential energy, momentum and contact count."""
+  by total kinetic and potential energy, momentum and contact count; the
+  same for 60 steps of the unified-memory step (evalForces, integrate with
+  the torus distance map, the cylinder and the planes) of the torus fall."""
 import numpy as np
 import pytest
 import torch
@@ -54,7 +56,7 @@ def test_packed_job_tables_bit_exact_every_step():
     assert nan > 0
 
 
-def _stats(pos, vel, params, radius_from_w):
+def _stats(pos, vel, params, radius_from_w, with_collider=True):
     from oracle import oracle as O
     v = vel[:, :3].astype(np.float64)
     ok = np.isfinite(pos[:, :3]).all(axis=1) & np.isfinite(v).all(axis=1)
@@ -64,7 +66,7 @@ def _stats(pos, vel, params, radius_from_w):
     h, x = O.calc_hash(params, pos)
     hs, xs = O.sort_pairs(h, x)
     cs, ce, sp, sv = O.reorder(hs, xs, pos, vel, params.numCells)
-    nv = O.collide(params, sp, sv, xs, cs, ce, radius_from_w)
+    nv = O.collide(params, sp, sv, xs, cs, ce, radius_from_w, with_collider)
     contacts = int(np.count_nonzero(np.any(nv[:, :3] != vel[:, :3], axis=1)))
     return ke, pe, mom, contacts
 
@@ -84,6 +86,38 @@ def test_packed_multistep_statistics_match_oracle():
     o = _stats(pos, vel, P, True)
     print(f"GPU ke {g[0]:.6e} pe {g[1]:.6e} contacts {g[3]}; "
           f"oracle ke {o[0]:.6e} pe {o[1]:.6e} contacts {o[3]}")
+    assert abs(g[0] - o[0]) <= 0.02 * o[0]
+    assert abs(g[1] - o[1]) <= 1e-3 * abs(o[1])
+    assert np.all(np.abs(g[2] - o[2]) <= 0.05 * np.abs(o[2]).max() + 1e-9)
+    assert abs(g[3] - o[3]) <= 0.02 * o[3]
+
+
+def test_um_torus_fall_statistics_match_oracle():
+    from fullc0ntact_gb300 import dem, scenes
+    from oracle import oracle as O
+    sc = scenes.torus_fall_scene(100_000, z0=0.09)  # the lowest layers start at the torus
+    dmap = dem.DistanceMap.torus(0.3, 0.1, 128, 0.05)
+    steps = 60
+    ds = dem.UmScene(sc, dmap)
+    ds.update(steps)
+    dem.check("um update")
+    P = oracle_params(bytes(sc["params"]))
+    w = bool(sc.get("radius_from_w", False))
+    v = dmap.vertices()
+    m = O.distmap_struct(dmap.vmin, dmap.vmax, dmap.cell_size, dmap.cells,
+                         np.ascontiguousarray(v[:, 0]), np.ascontiguousarray(v[:, 1:]))
+    pos, vel = sc["pos"].copy(), sc["vel"].copy()
+    for _ in range(steps):  # calcHash, sortParticles, reorder, evalForces, integrateSystem
+        h, x = O.calc_hash(P, pos)
+        hs, xs = O.sort_pairs(h, x)
+        cs, ce, sp, sv = O.reorder(hs, xs, pos, vel, P.numCells)
+        vel = O.collide(P, sp, sv, xs, cs, ce, w, False)
+        O.integrate_distmap(P, m, pos, vel, sc["dt"], w)
+    g = _stats(ds.pos.cpu().numpy(), ds.vel.cpu().numpy(), P, w, False)
+    o = _stats(pos, vel, P, w, False)
+    print(f"GPU ke {g[0]:.6e} pe {g[1]:.6e} contacts {g[3]}; "
+          f"oracle ke {o[0]:.6e} pe {o[1]:.6e} contacts {o[3]}")
+    assert o[3] > 1000  # the spheres are on the torus and on each other
     assert abs(g[0] - o[0]) <= 0.02 * o[0]
     assert abs(g[1] - o[1]) <= 1e-3 * abs(o[1])
     assert np.all(np.abs(g[2] - o[2]) <= 0.05 * np.abs(o[2]).max() + 1e-9)
