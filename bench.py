@@ -747,7 +747,13 @@ def run_ours(args):
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_source": peak_kind,
                          "traffic": traffic, "algorithmic_bytes": algo[dominant],
-                         "avg_launch_ms": stage_ms[dominant]},
+                         "avg_launch_ms": stage_ms[dominant],
+                         "note": ("collide is bound by instruction issue, not by DRAM: "
+                                  "61-65% issue-active with 13-16 of 32 lanes per "
+                                  "instruction at 2.6-5% DRAM throughput "
+                                  "(profiles/kCollideGlobal_packed_1M.md, "
+                                  "profiles/collide_settled_4M.md)")
+                         if dominant == "collide" else None},
             "stage_ms": stage_ms,
             "stage_roofline": stage_roofline,
             "step_roofline": step_roofline,
