@@ -442,11 +442,16 @@ __device__ void largeRadixPass(const unsigned long long *src, unsigned long long
   }
 }
 
-// The large cells listed by kFixupGather, one CTA per cell at a time.  The
-// members (particle index, previous entry) are sorted by particle index in
-// the cell's own range of sortedPos (16 bytes per member: two 8-byte arrays
-// of the cell's size), written back to slotOrig/slotPrev, then gathered as
-// in kFixupGather.  idBits = bits of the largest particle index.
+// The large cells listed by kFixupGather, one CTA per cell at a time.  A
+// CTA with a bitmap slot (blockIdx < kBitmapSlots) ranks a cell whose
+// members' index span is at most kBitmapSpan words per member with
+// bitmapRanks and gathers each member straight to its ranked place.
+// Otherwise the members (particle index, previous entry) are sorted by
+// particle index in the cell's own range of sortedPos (16 bytes per member:
+// two 8-byte arrays of the cell's size), written back to slotOrig/slotPrev,
+// then gathered as in kFixupGather.  idBits = bits of the largest particle
+// index; bitmaps = kBitmapSlots slots of 2 * bitmapWords(n) words (the bits,
+// then the word prefix), or nullptr for the sort only.
 __global__ void __launch_bounds__(kLargeThreads)
 kFixupLarge(unsigned *__restrict__ slotOrig, unsigned *__restrict__ slotPrev,
             const unsigned *__restrict__ off, const unsigned *__restrict__ large,
