@@ -9,7 +9,8 @@
 //           collide+integrate of the previous step, or kIntegrateHashCount)
 //           also takes r = atomicAdd(&cnt[h], 1) and counts h's 4096-cell
 //           tile in tileCnt;
-//   scan    kScanTiles (one CTA) scans the tile counts, kScanCells scans
+//   scan    kScanTiles (one CTA; above 8192 tiles kScanTileBlocks and
+//           kAddTileBlocks) scans the tile counts, kScanCells scans
 //           each tile's cells from its tile offset -- no inter-CTA waits; a
 //           tile without particles writes its constant offsets and skips
 //           reading cnt.  off = exclusive prefix sum of cnt over C + 1 cells,
@@ -27,8 +28,9 @@
 // holds what the reference's stages leave.  A cell with more than
 // kFixupMaxCell members is left out of the per-slot re-rank (its cost grows
 // with the square of the cell) and listed instead; kFixupLarge then gives each
-// listed cell one CTA that sorts its members by particle index with a stable
-// block radix sort, whatever the cell's size.
+// listed cell one CTA that ranks its members by particle index, whatever the
+// cell's size: with a bitmap of their indices when the indices are dense
+// enough, else with a stable block radix sort.
 #include "fcdem_dem.cuh"
 
 namespace fcdem {
