@@ -5,8 +5,9 @@
 // the keys; then each pass is a single "onesweep" kernel: a CTA takes the
 // next tile (4096 keys) from an atomic counter, ranks its keys stably by
 // digit with warp ballots, publishes its per-digit counts, resolves its
-// global offsets by decoupled look-back over the tiles before it, stages the
-// tile in shared memory in digit order and writes it out in runs.
+// global offsets by decoupled look-back over the tiles before it (each digit's
+// thread reads kLookWindow predecessors per round), stages the tile in shared
+// memory in digit order and writes it out in runs.
 //
 // Every look-back spin is bounded: after kSpinLimit polls the CTA records
 // kStatusTimeout in the device status word and carries on, so a fault in the
