@@ -459,11 +459,12 @@ __device__ __forceinline__ unsigned packBf16(float a, float b) {
   return (unsigned)__bfloat16_as_ushort(x) | ((unsigned)__bfloat16_as_ushort(y) << 16);
 }
 
-template <int H, int L>
+template <int H, int L, int T = 1>
 struct SdfTileSmem {
   static_assert(H == 64 || H == 128, "width");
   static_assert(L >= 2 && L <= 3, "hidden layers");
-  __nv_bfloat16 a[128 * H];            // activation tile (A operand)
+  static_assert(T == 1 || T == 2, "tiles per CTA");
+  __nv_bfloat16 a[T * 128 * H];        // activation tiles (A operands), 128 points each
   __nv_bfloat16 w[(L - 1) * H * H];    // hidden-layer weights (B operands)
   float w0[H * kSdfMaxInputs];         // first layer, [H][D]
   float b[L * H];                      // biases of the hidden layers
@@ -473,13 +474,13 @@ struct SdfTileSmem {
   unsigned long long bar;
 };
 
-// Per-CTA set-up of the tile forward: TMEM columns, the barrier, the
-// weights.  All threads of the CTA.
-template <int H, int L>
-__device__ __forceinline__ void sdfTileSetup(SdfTileSmem<H, L> &sm, const SdfView &net) {
+// Per-CTA set-up of the tile forward: TMEM columns (H per tile), the
+// barrier, the weights.  All threads of the CTA.
+template <int H, int L, int T = 1>
+__device__ __forceinline__ void sdfTileSetup(SdfTileSmem<H, L, T> &sm, const SdfView &net) {
   const int t = threadIdx.x;
   if (t < 32) {
-    tmemAlloc(smemU32(&sm.tmem), H);
+    tmemAlloc(smemU32(&sm.tmem), H * T);
     tmemRelinquish();
   }
   if (t == 0) {
@@ -503,25 +504,31 @@ __device__ __forceinline__ void sdfTileSetup(SdfTileSmem<H, L> &sm, const SdfVie
   tcFenceAfter();
 }
 
-template <int H, int L>
-__device__ __forceinline__ void sdfTileTeardown(SdfTileSmem<H, L> &sm) {
+template <int H, int L, int T = 1>
+__device__ __forceinline__ void sdfTileTeardown(SdfTileSmem<H, L, T> &sm) {
   tcFenceBefore();
   __syncthreads();
   if (threadIdx.x < 32) {
     tcFenceAfter();
-    tmemDealloc(sm.tmem, H);
+    tmemDealloc(sm.tmem, H * T);
   }
 }
 
 // The distance prediction for this thread's point (x normalised, shape code
-// `shape` or -1); 128 threads, one point each, all threads of the CTA.
-// `phase` is the barrier parity, flipped per MMA chain.  Returns false (for
-// every thread) when an MMA chain did not complete in time.
-template <int H, int L, int kLdBatch = 1>
-__device__ __forceinline__ bool sdfTileForward(SdfTileSmem<H, L> &sm, const SdfView &net,
+// `shape` or -1); 128 * T threads, one point each, all threads of the CTA.
+// Thread t works on tile t / 128, row t % 128: the tile's A operand is its
+// own 128-row block of sm.a and its accumulator TMEM columns tile * H ..,
+// read by the warp's lane quarter (warp % 4).  Every tile's chain uses the
+// same B operands and one commit.  `phase` is the barrier parity, flipped
+// per layer.  Returns false (for every thread) when an MMA chain did not
+// complete in time.
+template <int H, int L, int kLdBatch = 1, int T = 1>
+__device__ __forceinline__ bool sdfTileForward(SdfTileSmem<H, L, T> &sm, const SdfView &net,
                                                float x0, float x1, float x2, int shape,
                                                unsigned &phase, float &dOut) {
   const int t = threadIdx.x, warp = t >> 5;
+  const int tile = t >> 7, row = t & 127, quarter = warp & 3;
+  __nv_bfloat16 *aTile = sm.a + tile * 128 * H;
   const int D = net.lay.D;
   // first layer on the CUDA cores, 8 outputs per 16-byte chunk of the A row
 #pragma unroll 1
@@ -540,7 +547,7 @@ __device__ __forceinline__ bool sdfTileForward(SdfTileSmem<H, L> &sm, const SdfV
     }
     uint4 v = make_uint4(packBf16(h[0], h[1]), packBf16(h[2], h[3]), packBf16(h[4], h[5]),
                          packBf16(h[6], h[7]));
-    *reinterpret_cast<uint4 *>(sm.a + tileOffset(t, c * 8, 128)) = v;
+    *reinterpret_cast<uint4 *>(aTile + tileOffset(row, c * 8, 128)) = v;
   }
   proxyFence();
   tcFenceBefore();
@@ -555,9 +562,13 @@ __device__ __forceinline__ bool sdfTileForward(SdfTileSmem<H, L> &sm, const SdfV
       tcFenceAfter();
       const unsigned bBase = smemU32(sm.w + (l - 1) * H * H);
 #pragma unroll
-      for (int s = 0; s < H / 16; ++s)
-        umma(sm.tmem, umDesc(aBase + s * 2 * 128 * 16, 128 * 16, 128),
-             umDesc(bBase + s * 2 * H * 16, H * 16, 128), idesc, s > 0 ? 1u : 0u);
+      for (int tt = 0; tt < T; ++tt) {
+        const unsigned aTileBase = aBase + (unsigned)(tt * 128 * H * 2);
+#pragma unroll
+        for (int s = 0; s < H / 16; ++s)
+          umma(sm.tmem + (unsigned)(tt * H), umDesc(aTileBase + s * 2 * 128 * 16, 128 * 16, 128),
+               umDesc(bBase + s * 2 * H * 16, H * 16, 128), idesc, s > 0 ? 1u : 0u);
+      }
       ummaCommit(smemU32(&sm.bar));
     }
     const bool done = mbarWaitParity(smemU32(&sm.bar), phase);
@@ -579,7 +590,9 @@ __device__ __forceinline__ bool sdfTileForward(SdfTileSmem<H, L> &sm, const SdfV
       float r[kLdBatch][16];
 #pragma unroll
       for (int q = 0; q < kLdBatch; ++q)
-        tmemLoad16(sm.tmem + ((unsigned)(32 * warp) << 16) + (unsigned)((c0 + q) * 16), r[q]);
+        tmemLoad16(sm.tmem + ((unsigned)(32 * quarter) << 16) +
+                       (unsigned)(tile * H + (c0 + q) * 16),
+                   r[q]);
       tmemWaitLoad();
 #pragma unroll
       for (int q = 0; q < kLdBatch; ++q) {
@@ -596,7 +609,7 @@ __device__ __forceinline__ bool sdfTileForward(SdfTileSmem<H, L> &sm, const SdfV
                                  packBf16(r[q][8 * h + 2], r[q][8 * h + 3]),
                                  packBf16(r[q][8 * h + 4], r[q][8 * h + 5]),
                                  packBf16(r[q][8 * h + 6], r[q][8 * h + 7]));
-            *reinterpret_cast<uint4 *>(sm.a + tileOffset(t, c * 16 + 8 * h, 128)) = v;
+            *reinterpret_cast<uint4 *>(aTile + tileOffset(row, c * 16 + 8 * h, 128)) = v;
           }
         }
       }
@@ -610,30 +623,35 @@ __device__ __forceinline__ bool sdfTileForward(SdfTileSmem<H, L> &sm, const SdfV
 }
 
 // d[i] for point i (float4, w ignored) with shape code shapes[i] (or none).
+// kInferTiles 128-point tiles per CTA share the weights and one barrier
+// round per layer; inferLd<H>() TMEM column loads are in flight per wait.
+constexpr int kInferTiles = 2;
+template <int H> constexpr int inferLd() { return H == 64 ? 2 : 4; }
 template <int H, int L>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128 * kInferTiles)
 kSdfInfer(SdfView net, const float4 *__restrict__ pts, const int *__restrict__ shapes,
           unsigned n, float *__restrict__ dOut, unsigned *status) {
   extern __shared__ __align__(1024) unsigned char smraw[];
-  SdfTileSmem<H, L> &sm = *reinterpret_cast<SdfTileSmem<H, L> *>(smraw);
-  sdfTileSetup<H, L>(sm, net);
+  SdfTileSmem<H, L, kInferTiles> &sm =
+      *reinterpret_cast<SdfTileSmem<H, L, kInferTiles> *>(smraw);
+  sdfTileSetup<H, L, kInferTiles>(sm, net);
   unsigned phase = 0;
-  const unsigned tiles = (n + 127) / 128;
-  for (unsigned tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-    const unsigned i = tile * 128 + threadIdx.x;
+  const unsigned groups = (n + 128u * kInferTiles - 1) / (128u * kInferTiles);
+  for (unsigned g = blockIdx.x; g < groups; g += gridDim.x) {
+    const unsigned i = g * 128u * kInferTiles + threadIdx.x;
     const bool valid = i < n;
     const float4 q = valid ? __ldg(pts + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const int shape = (valid && shapes) ? __ldg(shapes + i) : -1;
     float d = 0.0f;
-    if (!sdfTileForward<H, L, 4>(sm, net, (q.x - net.shift[0]) * net.scale[0],
-                              (q.y - net.shift[1]) * net.scale[1],
-                              (q.z - net.shift[2]) * net.scale[2], shape, phase, d)) {
+    if (!sdfTileForward<H, L, inferLd<H>(), kInferTiles>(
+            sm, net, (q.x - net.shift[0]) * net.scale[0], (q.y - net.shift[1]) * net.scale[1],
+            (q.z - net.shift[2]) * net.scale[2], shape, phase, d)) {
       if (threadIdx.x == 0) atomicOr(status, (unsigned)kStatusTimeout);
       break;
     }
     if (valid) dOut[i] = d;
   }
-  sdfTileTeardown<H, L>(sm);
+  sdfTileTeardown<H, L, kInferTiles>(sm);
 }
 
 // Per-tile hints of the culling kernels (performance only: results never
@@ -952,12 +970,42 @@ constexpr unsigned sdfCtasPerSm() {
 template <int H, int L>
 bool launchInfer(fcdemSdfNet *net, const float4 *pts, const int *shapes, unsigned n,
                  float *d) {
-  const size_t smem = tileSmemBytes<H, L>();
-  cudaFuncSetAttribute(kSdfInfer<H, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  unsigned grid = (n + 127) / 128;
-  if (grid > 152u * sdfCtasPerSm<H, L>()) grid = 152u * sdfCtasPerSm<H, L>();
-  kSdfInfer<H, L><<<grid, 128, smem, curStream()>>>(sdfView(net), pts, shapes, n, d,
-                                                    ctx().dStatus);
+  const size_t smem = sizeof(SdfTileSmem<H, L, kInferTiles>) + 1024;  // + alignment slack
+  const int threads = 128 * kInferTiles;
+  // persistent grid: the CTAs that are resident at once (registers, shared
+  // memory), capped by the 512 TMEM columns of an SM (H per tile): a CTA
+  // beyond that would wait in tcgen05.alloc for columns no CTA frees.
+  // Worked out once per device (the attribute calls cost more host time
+  // than a launch).
+  static int residentOf[64] = {};
+  int dev = 0;
+  if (!cudaOk(cudaGetDevice(&dev))) return false;
+  if (dev < 0 || dev >= 64) dev = 0;
+  int resident = residentOf[dev];
+  if (resident == 0) {
+    // the whole carveout as shared memory
+    if (!cudaOk(cudaFuncSetAttribute(kSdfInfer<H, L>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) ||
+        !cudaOk(cudaFuncSetAttribute(kSdfInfer<H, L>,
+                                     cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     (int)cudaSharedmemCarveoutMaxShared)))
+      return false;
+    cudaFuncAttributes fa;
+    if (!cudaOk(cudaFuncGetAttributes(&fa, kSdfInfer<H, L>))) return false;
+    // registers are allocated per warp in units of 256
+    const int regsPerWarp = ((fa.numRegs * 32 + 255) / 256) * 256;
+    const int byRegs = regsPerWarp > 0 ? (65536 / regsPerWarp) / (threads / 32) : 1;
+    const int bySmem = (int)((227u * 1024u) / (smem + 1024u));  // + the per-CTA reserve
+    const int byTmem = 512 / (H * kInferTiles);
+    resident = byRegs < bySmem ? byRegs : bySmem;
+    if (resident > byTmem) resident = byTmem;
+    if (resident < 1) resident = 1;
+    residentOf[dev] = resident;
+  }
+  unsigned grid = (n + 128u * kInferTiles - 1) / (128u * kInferTiles);
+  if (grid > 152u * (unsigned)resident) grid = 152u * (unsigned)resident;
+  kSdfInfer<H, L><<<grid, threads, smem, curStream()>>>(sdfView(net), pts, shapes, n, d,
+                                                        ctx().dStatus);
   return launchOk();
 }
 

@@ -142,6 +142,26 @@ def test_tensor_core_inference_matches_bf16_reference(cfg):
     assert float((d - f32).abs().max()) <= 3e-2 * scale
 
 
+@pytest.mark.parametrize("cfg", [(3, 64, 3), (11, 128, 2)])
+def test_inference_is_independent_of_the_tile(cfg):
+    """kSdfInfer runs two 128-point tiles per CTA (one per TMEM column
+    block).  Shifting the points by 128 moves each into the other tile: the
+    predictions keep their bits, so both tiles compute what the one-tile
+    forward of the fused culling kernels computes."""
+    from fullc0ntact_gb300 import sdf
+    dmap = _torus()
+    net = _net(*cfg, dmap, jitter=0.05)
+    n = 70_000
+    s = sdf.samples(dmap, n, 0.3, 0.05, seed=6)
+    g = torch.Generator(device="cuda").manual_seed(9)
+    shapes = (torch.randint(0, cfg[0] - 3, (n,), device="cuda", dtype=torch.int32, generator=g)
+              if cfg[0] > 3 else None)
+    a = net.infer(s, shapes).clone()
+    b = net.infer(s[128:].contiguous(), None if shapes is None else shapes[128:].contiguous())
+    np.testing.assert_array_equal(a[128:].cpu().numpy().view(np.uint32),
+                                  b.cpu().numpy().view(np.uint32))
+
+
 def test_trained_network_culls_exact_queries_without_changing_results():
     """Config-2 network (3 -> 64 -> 64 -> 64 -> 1) trained on 2M samples of
     the 128^3 torus map.  Judged by the exact map: no point the map puts
