@@ -196,3 +196,21 @@ def test_inert_particles_identical_on_every_path(pipeline):
     b = _run_crowd(sc, False, 5, pipeline)
     for x, y in zip(a, b):
         np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
+
+
+@pytest.mark.parametrize("limit", [128, 2048])
+def test_crowd_limit_does_not_change_results(limit):
+    """The neighbourhood size above which a particle goes to the crowded
+    kernel (fcdemSetCrowdLimit) moves work between the two kernels only:
+    three fused updates of the packed scene with crowded cells end in the
+    same bits at the default limit (512) and at `limit`."""
+    from fullc0ntact_gb300 import dem
+    sc = _crowded_scene("packed")
+    a = _run_crowd(sc, True, 3)
+    dem.lib.fcdemSetCrowdLimit(limit)
+    try:
+        b = _run_crowd(sc, True, 3)
+    finally:
+        dem.lib.fcdemSetCrowdLimit(0)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
