@@ -18,9 +18,11 @@ copyArrayFromDevice of pos and vel.  The working set (~560 MB) exceeds the
 
 --impl reference times the reference's CPU implementation of the step (the C
 restatement of cuda_addon/particles_kernel.cu in oracle/, using all host
-threads for the collide stage) on a bounded sample: each step is one full
-update of the same scene.  Multi-GPU (torchrun): independent replicas, one per
-rank, no collective on the data path; value sums the ranks' particle-steps.
+threads for the collide stage) on a bounded sample: the first steps of the
+same job from the same packed state, each one full update.  It builds the
+scene with the oracle build of the scene generators and never loads the GPU
+library.  Multi-GPU (torchrun): independent replicas, one per rank, no
+collective on the data path; value sums the ranks' particle-steps.
 """
 from __future__ import annotations
 
@@ -75,15 +77,30 @@ def parse():
     ap.add_argument("--obstacle-scenes", type=int, default=128)
     ap.add_argument("--obstacle-steps", type=int, default=500)
     ap.add_argument("--batch-scenes", type=int, default=512)
-    ap.add_argument("--batch-steps", type=int, default=20)
+    ap.add_argument("--batch-steps", type=int, default=1000,
+                    help="steps of the batched job (512 scenes, a 1000-step job)")
+    ap.add_argument("--batch-plain-steps", type=int, default=100,
+                    help="steps over which the batch and the scenes one at a time are compared")
+    ap.add_argument("--no-ref-gpu", action="store_true",
+                    help="skip timing the reference's own GPU kernels")
+    ap.add_argument("--ref-gpu-steps", type=int, default=200)
     return ap.parse_args()
+
+
+def job_config(args, n: int) -> dict:
+    """The workload as both arms name it (the same dict in both lines)."""
+    return {"workload": f"{WORKLOAD}, {args.steps}-step job from the packed state"
+                        + (f" advanced by {args.advance} steps" if args.advance else ""),
+            "n": n, "grid": 256, "cells": 256 ** 3,
+            "l2": "inputs larger than L2 (no flush)",
+            "parallelism": f"replicas x{dist_env()[0]}"}
 
 
 def load_scene(n: int) -> dict:
     """The packed 4,194,304-sphere scene, cached on local disk (packing 4M spheres takes ~15 s)."""
     from fullc0ntact_gb300 import scenes
     from fullc0ntact_gb300.params import SimParams
-    path = os.path.join(tempfile.gettempdir(), f"fcdem_scene_packed_{n}_v2.npz")
+    path = os.path.join(tempfile.gettempdir(), f"fcdem_scene_packed_{n}_v3.npz")
     if os.path.exists(path):
         try:
             with np.load(path) as z:
@@ -211,47 +228,190 @@ def load_batch(num_scenes: int) -> list:
     return sl
 
 
-def measure_batched(num_scenes: int, steps: int, dev: int) -> dict:
-    """The same scenes stepped (a) all together as one batch, replayed from a
-    CUDA graph, and (b) one scene after the other with its own launches (the
-    plain step): particle-steps/s of each, CUDA events on the stream."""
+def measure_batched(num_scenes: int, steps: int, plain_steps: int, dev: int) -> dict:
+    """The batched job: all scenes stepped together, replayed from a CUDA
+    graph, `steps` steps from the packed states.  Then, over the first
+    `plain_steps` steps, the batch against the same scenes stepped one after
+    the other with their own launches (the plain step).  And the floor of a
+    graph-replayed step: the same number of scenes with 32 spheres each
+    (launch gaps and near-empty kernels), which bounds what folding a step's
+    launches into one persistent launch could save."""
     import torch
-    from fullc0ntact_gb300 import dem
+    from fullc0ntact_gb300 import dem, scenes
     sl = load_batch(num_scenes)
     n_total = sum(s["pos"].shape[0] for s in sl)
-    batch = dem.Batch(sl, f"cuda:{dev}")
-    batch.update(2, graph=True)  # records the 2-step graph, warms up
-    batch.update(steps, graph=True)  # records the timed graph
-    torch.cuda.synchronize()
+    pos0 = torch.from_numpy(np.concatenate([s["pos"] for s in sl]))
+    vel0 = torch.from_numpy(np.concatenate([s["vel"] for s in sl]))
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    batch.update(steps, graph=True)
-    e1.record()
-    torch.cuda.synchronize()
-    batched_ms = e0.elapsed_time(e1)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    batch = dem.Batch(sl, f"cuda:{dev}")
+    batch.update(2, graph=True)  # warm-up
+    batch.update(steps, graph=True)  # records the job's graph
+    batch.pos.copy_(pos0)
+    batch.vel.copy_(vel0)
+    job_ms = timed(lambda: batch.update(steps, graph=True))
+    dem.check("batched job")
+    batch.update(plain_steps, graph=True)  # records the comparison graph
+    batch.pos.copy_(pos0)
+    batch.vel.copy_(vel0)
+    batched_ms = timed(lambda: batch.update(plain_steps, graph=True))
     dem.check("batched")
+    del batch
     singles = [dem.Batch([sc], f"cuda:{dev}") for sc in sl]
     for b in singles:
-        b.update(1, graph=False)
-    torch.cuda.synchronize()
-    e0.record()
-    for b in singles:
-        b.update(steps, graph=False)
-    e1.record()
-    torch.cuda.synchronize()
-    plain_ms = e0.elapsed_time(e1)
+        b.update(1, graph=False)  # warm-up
+    for b, sc in zip(singles, sl):
+        b.pos.copy_(torch.from_numpy(sc["pos"]))
+        b.vel.copy_(torch.from_numpy(sc["vel"]))
+
+    def run_singles():
+        for b in singles:
+            b.update(plain_steps, graph=False)
+    plain_ms = timed(run_singles)
     dem.check("plain per scene")
+    del singles
+    tiny = [scenes.batch_scene(32, 77 + k) for k in range(num_scenes)]
+    tb = dem.Batch(tiny, f"cuda:{dev}")
+    tb.update(plain_steps, graph=True)
+    floor_ms = timed(lambda: tb.update(plain_steps, graph=True)) / plain_steps
+    dem.check("graph floor")
+    del tb
     sizes = [s["pos"].shape[0] for s in sl]
-    bv = n_total * steps / (batched_ms / 1e3)
-    pv = n_total * steps / (plain_ms / 1e3)
+    bv = n_total * plain_steps / (batched_ms / 1e3)
+    pv = n_total * plain_steps / (plain_ms / 1e3)
     return {"workload": f"{num_scenes} scenes, sizes log-uniform in [1024, 65536], radii "
-                        "U[1/512, 1/256], 25% volume fraction, own box and grid each",
+                        "U[1/512, 1/256], 25% volume fraction, own box and grid each, "
+                        f"{steps}-step job",
             "n_total": n_total, "scene_min": int(min(sizes)), "scene_max": int(max(sizes)),
-            "cells_total": batch.num_cells, "steps": steps,
-            "batched_graph": {"value": bv, "ms_per_step": batched_ms / steps},
-            "plain_per_scene": {"value": pv, "ms_per_step": plain_ms / steps},
+            "cells_total": int(sum(int(s["params"].numCells) for s in sl)), "steps": steps,
+            "job_batched_graph": {"value": n_total * steps / (job_ms / 1e3),
+                                  "ms_per_step": job_ms / steps},
+            "first_steps": plain_steps,
+            "batched_graph": {"value": bv, "ms_per_step": batched_ms / plain_steps},
+            "plain_per_scene": {"value": pv, "ms_per_step": plain_ms / plain_steps},
             "speedup": bv / pv, "unit": UNIT,
+            "graph_step_floor_ms": floor_ms,
+            "graph_step_floor_share": floor_ms / (batched_ms / plain_steps),
             "equal_results": "bit-identical per scene (tests/test_gpu_batch.py)"}
+
+
+def measure_reference_gpu(steps: int, dev: int) -> dict:
+    """The reference's own GPU step on this GPU: cuda_addon/particles_kernel.cu
+    compiled for sm_103a (oracle/_ref/fcref_kernels.cubin) under its launch
+    glue restated (particleSystem.cu:123-270: setParameters each update, 256
+    threads for integrate, calcHash and reorder, 64 for collide, the 0xff
+    memset of cellStart, thrust::sort_by_key), next to the product's plain
+    step on the same scenes from the same state: the five reference-named
+    calls, fcdemUpdate (fused), and the one-scene batch replayed from a CUDA
+    graph.  Monodisperse scenes only (the reference's collide has one
+    radius): the 16,384-sphere lattice (64^3 cells, 1,000 steps) and the
+    1,048,576 spheres of radius 1/256 of the torus fall, without the
+    obstacle (256^3 cells): the reference's distance-map step
+    (particledem_um.cu) needs Eigen and does not build."""
+    import torch
+    from fullc0ntact_gb300 import dem, scenes
+    from oracle import oracle as O
+    try:
+        R = O.ref_gpu()
+    except RuntimeError as e:
+        return {"unavailable": str(e)}
+    S = O.ref_thrust_sort()
+    if R is None or S is None:
+        return {"unavailable": "the reference cubin or the Thrust sort glue was not built"}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    out = {}
+    cases = [("lattice_16k", scenes.lattice_scene(16384), 1000),
+             ("monodisperse_1m", scenes.torus_fall_scene(1_048_576), steps)]
+    for name, sc, k in cases:
+        n = sc["pos"].shape[0]
+        P = O.SimParams.from_buffer_copy(bytes(sc["params"]))
+        pos = torch.from_numpy(sc["pos"]).to(f"cuda:{dev}")
+        vel = torch.from_numpy(sc["vel"]).to(f"cuda:{dev}")
+        h = torch.empty(n, dtype=torch.int32, device=pos.device)
+        x = torch.empty_like(h)
+        cs = torch.empty(P.numCells, dtype=torch.int32, device=pos.device)
+        ce = torch.full((P.numCells,), -1, dtype=torch.int32, device=pos.device)
+        sp, sv = torch.empty_like(pos), torch.empty_like(vel)
+
+        def ref_step():
+            R.fcrefgpu_set_parameters(C.byref(P))
+            R.fcrefgpu_integrate(pos.data_ptr(), vel.data_ptr(), sc["dt"], n, None)
+            R.fcrefgpu_calc_hash(h.data_ptr(), x.data_ptr(), pos.data_ptr(), n, None)
+            S.fcrefgpu_sort_by_key(h.data_ptr(), x.data_ptr(), n)
+            R.fcrefgpu_reorder(cs.data_ptr(), ce.data_ptr(), sp.data_ptr(), sv.data_ptr(),
+                               h.data_ptr(), x.data_ptr(), pos.data_ptr(), vel.data_ptr(), n,
+                               P.numCells, None)
+            R.fcrefgpu_collide(vel.data_ptr(), sp.data_ptr(), sv.data_ptr(), x.data_ptr(),
+                               cs.data_ptr(), ce.data_ptr(), n, None)
+
+        for _ in range(3):
+            ref_step()
+        pos.copy_(torch.from_numpy(sc["pos"]))
+        vel.copy_(torch.from_numpy(sc["vel"]))
+
+        def ref_job():
+            for _ in range(k):
+                ref_step()
+        ref_ms = timed(ref_job)
+        assert R.fcrefgpu_sync() == 0
+        del pos, vel, h, x, cs, ce, sp, sv
+        ds = dem.DeviceScene(sc, f"cuda:{dev}")
+        for _ in range(3):
+            ds.stages()
+        ds.pos.copy_(torch.from_numpy(sc["pos"]))
+        ds.vel.copy_(torch.from_numpy(sc["vel"]))
+
+        def staged():
+            for _ in range(k):
+                ds.stages()
+        staged_ms = timed(staged)
+        dem.check("staged")
+        ds.update(3)
+        ds.pos.copy_(torch.from_numpy(sc["pos"]))
+        ds.vel.copy_(torch.from_numpy(sc["vel"]))
+        fused_ms = timed(lambda: ds.update(k))
+        dem.check("fused")
+        del ds
+        one = dict(sc, box_lo=np.array([-1.0] * 3, np.float32),
+                   box_hi=np.array([1.0] * 3, np.float32))
+        b = dem.Batch([one], f"cuda:{dev}")
+        b.update(k, graph=True)
+        b.pos.copy_(torch.from_numpy(sc["pos"]))
+        b.vel.copy_(torch.from_numpy(sc["vel"]))
+        graph_ms = timed(lambda: b.update(k, graph=True))
+        dem.check("graph")
+        del b
+        torch.cuda.empty_cache()
+
+        def v(ms):
+            return {"value": n * k / (ms / 1e3), "ms_per_step": ms / k}
+        out[name] = {"n": n, "cells": int(P.numCells), "steps": k, "unit": UNIT,
+                     "reference_gpu": v(ref_ms), "staged_calls": v(staged_ms),
+                     "fused_update": v(fused_ms), "graph_replayed": v(graph_ms),
+                     "fused_over_reference": ref_ms / fused_ms,
+                     "graph_over_reference": ref_ms / graph_ms}
+    out["note"] = ("reference kernels: the reference's own particles_kernel.cu for sm_103a; "
+                   "integrate launched per element with 256 threads (the reference uses "
+                   "thrust::for_each); results of one step agree with the product's to the "
+                   "force tolerance (tests/test_gpu_refkernels.py)")
+    return out
 
 
 def measured_peak_tflops():
@@ -521,18 +681,25 @@ def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
         return 0
+    from oracle import oracle as O
+    from fullc0ntact_gb300 import scenes
+    scenes.use_generator(O.scenegen())  # the workload without the GPU library
     sc = load_scene(args.n)
     n = sc["pos"].shape[0]
-    from oracle import oracle as O
     P = O.SimParams.from_buffer_copy(bytes(sc["params"]))
-    pos, vel = sc["pos"].copy(), sc["vel"].copy()
     threads = os.cpu_count() or 1
+    pos, vel = sc["pos"].copy(), sc["vel"].copy()
+    if args.advance > 0:
+        O.update(P, pos, vel, sc["dt"], steps=args.advance, radius_from_w=True, nthreads=threads)
+    pos0, vel0 = pos.copy(), vel.copy()
     t0 = time.perf_counter()
     O.update(P, pos, vel, sc["dt"], steps=max(args.warmup, 1), radius_from_w=True,
              nthreads=threads)
     per_step = (time.perf_counter() - t0) / max(args.warmup, 1)
-    # bounded sample: all K steps unless they would exceed the time cap
+    # bounded sample: all K steps unless they would exceed the time cap; from
+    # the state the GPU arm's timed job starts from
     steps = max(1, min(args.steps, int(args.cpu_budget_s / max(per_step, 1e-9))))
+    pos, vel = pos0.copy(), vel0.copy()
     t0 = time.perf_counter()
     O.update(P, pos, vel, sc["dt"], steps=steps, radius_from_w=True, nthreads=threads)
     el = time.perf_counter() - t0
@@ -542,13 +709,12 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded packing)",
-        "config": {"workload": f"{WORKLOAD}, {args.steps}-step job from the packed state",
-                   "n": n, "grid": 256, "l2": "inputs larger than L2 (no flush)"},
+        "config": job_config(args, n),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{steps} of {args.steps} steps timed, each a full update "
-                                   f"of the {n}-sphere scene (collide on {threads} threads, "
-                                   f"other stages on 1), from the start of the job: the "
-                                   f"cheapest steps of it (later ones hold crowded cells)"},
+                         "sample": f"the first {steps} of the job's {args.steps} steps, each a "
+                                   f"full update of the {n}-sphere scene from the packed "
+                                   f"state (collide on {threads} threads, other stages on 1); "
+                                   f"later steps of the job hold crowded cells and cost more"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -720,11 +886,17 @@ def run_ours(args):
         batched_obstacles = measure_batched_obstacles(args.obstacle_scenes, args.obstacle_steps, dev)
         torch.cuda.empty_cache()
 
+    ref_gpu = None
+    if not args.no_ref_gpu:
+        ref_gpu = measure_reference_gpu(args.ref_gpu_steps, dev)
+        torch.cuda.empty_cache()
+
     batched = None
     if not args.no_batched:
         del ds  # free the large scene's arrays first
         torch.cuda.empty_cache()
-        batched = measure_batched(args.batch_scenes, args.batch_steps, dev)
+        batched = measure_batched(args.batch_scenes, args.batch_steps, args.batch_plain_steps,
+                                  dev)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline and world == 1:
@@ -736,13 +908,9 @@ def run_ours(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": el_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded packing)",
-            "config": {"workload": f"{WORKLOAD}, {args.steps}-step job from the packed state"
-                                   + (f" advanced by {args.advance} steps" if args.advance else ""),
-                       "n": n, "grid": 256, "cells": ncell,
-                       "occupied_cells": occupied, "step": "fcdemUpdate (fused update)",
-                       "sort_config": sort_cfg, "cell_order": args.cell_order,
-                       "l2": "inputs larger than L2 (no flush)",
-                       "parallelism": f"replicas x{world}"},
+            "config": job_config(args, n),
+            "job": {"occupied_cells": occupied, "step": "fcdemUpdate (fused update)",
+                    "sort_config": sort_cfg, "cell_order": args.cell_order},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
                     "d2h_bytes_per_step": 2 * nbytes, "steps": e2e_steps,
                     "path": "copyArrayToDevice x2, fcdemUpdate, copyArrayFromDevice x2"},
@@ -752,12 +920,8 @@ def run_ours(args):
                          "peak_source": peak_kind,
                          "traffic": traffic, "algorithmic_bytes": algo[dominant],
                          "avg_launch_ms": stage_ms[dominant],
-                         "note": ("collide is bound by instruction issue, not by DRAM: "
-                                  "61-65% issue-active with 13-16 of 32 lanes per "
-                                  "instruction at 2.6-5% DRAM throughput "
-                                  "(profiles/kCollideGlobal_packed_1M.md, "
-                                  "profiles/collide_settled_4M.md)")
-                         if dominant == "collide" else None},
+                         "share_of_step": stage_ms[dominant] / sum(
+                             v for v in stage_ms.values() if v)},
             "stage_ms": stage_ms,
             "stage_roofline": stage_roofline,
             "step_roofline": step_roofline,
@@ -766,6 +930,7 @@ def run_ours(args):
             "batched": batched,
             "torus_obstacle": torus_obstacle,
             "batched_obstacles": batched_obstacles,
+            "reference_gpu": ref_gpu,
             "clocks": clk,
             "cpu_baseline": cpu,
         }

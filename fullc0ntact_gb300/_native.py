@@ -58,6 +58,7 @@ _SIGS = {
     "fcdemSetUpdatePipeline": (None, [C.c_int]),
     "fcdemAutotuneSort": (C.c_int, [C.c_uint, C.c_uint, C.POINTER(C.c_float)]),
     "fcdemSetSortConfig": (C.c_int, [C.c_uint, C.c_int]),
+    "fcdemSetSortWaitLimit": (None, [C.c_int]),
 }
 
 for _name, (_res, _args) in _SIGS.items():

@@ -25,7 +25,11 @@ SOURCES = [
     "fcdem_batch.cu",
     "fcdem_sdf.cu",
     "fcdem_host.cpp",
+    "fcdem_scenes.cpp",
 ]
+# per-file host-compiler flags (the scene generators round every a*b+c
+# twice, as the reference arm's build of the same file does)
+EXTRA = {"fcdem_scenes.cpp": ["-Xcompiler", "-ffp-contract=off"]}
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = [
@@ -67,7 +71,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         o = os.path.join(BUILD, src.replace(".cu", ".o").replace(".cpp", ".o"))
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            cmd = [cc] + ARCH + NVFLAGS + ["-c", s, "-o", o]
+            cmd = [cc] + ARCH + NVFLAGS + EXTRA.get(src, []) + ["-c", s, "-o", o]
             jobs.append(cmd)
 
     def run(cmd):

@@ -782,7 +782,7 @@ kCollideTiled(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
 
 bool g_crowdPath = true;  // fcdemSetCrowdPath
 unsigned g_crowdLimit = kCrowdLimit;  // fcdemSetCrowdLimit
-constexpr unsigned kCrowdCtas = 152 * 4;
+constexpr unsigned kCrowdCtasPerSm = 4;  // persistent grid: this many CTAs per SM
 
 // The group list for n particles (grown on demand; at most one group per
 // particle), its counters cleared on the current stream.  groups == nullptr
@@ -826,7 +826,7 @@ void launchT(bool tiled, bool cull, unsigned n, float4 *newVel, const float4 *sp
                                           crowd, ctx().dStatus);
     if (crowd.groups && launchOk())
       kCollideCrowd<kMode, kRadiusFromW, kCollider, kForceOut, kPrefix>
-          <<<kCrowdCtas, kCrowdWarps * 32, 0, curStream()>>>(newVel, sp, sv, index, cells, n,
+          <<<numSms() * kCrowdCtasPerSm, kCrowdWarps * 32, 0, curStream()>>>(newVel, sp, sv, index, cells, n,
                                                              kp, out, cull, crowd,
                                                              ctx().dStatus);
   }

@@ -1,5 +1,5 @@
 // fcdem_context.cu -- per-device state, error reporting and the support
-// entry points of the reference's C interface (particleSystem.cu:99-190).
+// entry points of the reference's C interface (particleSystem.cu:36-127).
 #include <atomic>
 #include <cstdio>
 #include <vector>
@@ -97,15 +97,38 @@ Context &ctx() {
   return c;
 }
 
-const Context *ctxIfCreated() {
+bool paramsIfSet(SimParams &out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) {
     cudaGetLastError();
-    return nullptr;
+    return false;
   }
-  if (dev < 0 || dev >= kMaxDevices) return nullptr;
+  if (dev < 0 || dev >= kMaxDevices) return false;
+  std::lock_guard<std::mutex> lock(g_mutex);
   const Context &c = g_ctx[dev];
-  return c.device >= 0 ? &c : nullptr;
+  if (c.device < 0 || !c.haveParams) return false;
+  out = c.params;
+  return true;
+}
+
+unsigned numSms() {
+  static std::atomic<int> sms[kMaxDevices];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    dev = -1;
+  }
+  if (dev >= 0 && dev < kMaxDevices) {
+    int v = sms[dev].load(std::memory_order_relaxed);
+    if (v > 0) return (unsigned)v;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+        v > 0) {
+      sms[dev].store(v, std::memory_order_relaxed);
+      return (unsigned)v;
+    }
+    cudaGetLastError();
+  }
+  return 152u;  // GB300 (not reached on a working device)
 }
 
 void *scratch(Context &c, size_t bytes) {
@@ -216,30 +239,43 @@ void unmapGLBufferObject(struct cudaGraphicsResource *) {
 void setParameters(SimParams *hostParams) {
   if (!hostParams) { setError(FCDEM_ERR_INVALID_VALUE); return; }
   Context &c = ctx();
+  std::lock_guard<std::mutex> lock(g_mutex);
   c.params = *hostParams;
   c.haveParams = true;
 }
 
+}  // extern "C"
+
+namespace {
+// Reads and clears a device status word (synchronising the library stream)
+// and records the first error its bits stand for.
+void drainStatus(unsigned *word) {
+  unsigned status = 0;
+  cudaStream_t s = curStream();
+  if (cudaMemcpyAsync(&status, word, sizeof(unsigned), cudaMemcpyDeviceToHost, s) ==
+          cudaSuccess &&
+      cudaStreamSynchronize(s) == cudaSuccess) {
+    if (status) {
+      cudaMemsetAsync(word, 0, sizeof(unsigned), s);
+      if (status & kStatusTimeout) setError(FCDEM_ERR_DEVICE_TIMEOUT);
+      else if (status & kStatusKeyRange) setError(FCDEM_ERR_KEY_RANGE);
+      else if (status & kStatusRadiusBound) setError(FCDEM_ERR_RADIUS_BOUND);
+      else if (status & kStatusCellOverflow) setError(FCDEM_ERR_CELL_OVERFLOW);
+    }
+  } else {
+    cudaGetLastError();
+    setError(FCDEM_ERR_CUDA);
+  }
+}
+}  // namespace
+
+extern "C" {
+
 int fcdemGetLastError(void) {
   Context &c = ctx();
-  if (c.dStatus) {
-    unsigned status = 0;
-    cudaStream_t s = curStream();
-    if (cudaMemcpyAsync(&status, c.dStatus, sizeof(unsigned),
-                        cudaMemcpyDeviceToHost, s) == cudaSuccess &&
-        cudaStreamSynchronize(s) == cudaSuccess) {
-      if (status) {
-        cudaMemsetAsync(c.dStatus, 0, sizeof(unsigned), s);
-        if (status & kStatusTimeout) setError(FCDEM_ERR_DEVICE_TIMEOUT);
-        else if (status & kStatusKeyRange) setError(FCDEM_ERR_KEY_RANGE);
-        else if (status & kStatusRadiusBound) setError(FCDEM_ERR_RADIUS_BOUND);
-        else if (status & kStatusCellOverflow) setError(FCDEM_ERR_CELL_OVERFLOW);
-      }
-    } else {
-      cudaGetLastError();
-      setError(FCDEM_ERR_CUDA);
-    }
-  }
+  if (c.dStatus) drainStatus(c.dStatus);
+  // the allocation-free sort keeps its own status word in its static scratch
+  if (unsigned *w = noAllocStatusWord()) drainStatus(w);
   return g_error.exchange(FCDEM_SUCCESS);
 }
 

@@ -1,7 +1,7 @@
 // fcdem_count.cu -- the cell counting-sort pipeline of fcdemUpdate.
 //
 // The reference re-sorts all particles by cell hash every step
-// (thrust::sort_by_key, particleSystem.cu:328-333) and then scatters the
+// (thrust::sort_by_key, particleSystem.cu:265-270) and then scatters the
 // cell ranges (reorderDataAndFindCellStartD).  Inside fcdemUpdate the same
 // result comes from a counting sort over the cells:
 //
@@ -313,7 +313,6 @@ kFixupGather(const unsigned *__restrict__ slotKey, const unsigned *__restrict__ 
 
 constexpr int kLargeThreads = 1024;
 constexpr int kLargeWarps = kLargeThreads / 32;
-constexpr int kLargeCtas = 152;
 constexpr int kBitmapSlots = 16;  // CTAs of kFixupLarge that own a bitmap
 
 // Words of one bitmap slot: a presence bit per particle index.
@@ -755,7 +754,7 @@ bool countPipelineSort(Context &c, const CountBuffers &b, const unsigned *origOf
                                                  n, numCells, b.large, b.largeCap, c.dStatus);
   if (!launchOk()) return false;
   // Returns at once when the fix-up listed no cell (the common case).
-  const unsigned largeCtas = b.largeCap < (unsigned)kLargeCtas ? b.largeCap : kLargeCtas;
+  const unsigned largeCtas = b.largeCap < numSms() ? b.largeCap : numSms();  // one per SM at most
   kFixupLarge<<<largeCtas, kLargeThreads, 0, st>>>(b.slotIdx, b.slotPrev, b.off, b.large,
                                                    b.largeCap, hash, index, sortedPos,
                                                    sortedVel, prevPos, prevVel, n, keyBits(n),
@@ -766,7 +765,7 @@ bool countPipelineSort(Context &c, const CountBuffers &b, const unsigned *origOf
 bool countPipelineTables(const CountBuffers &b, unsigned *cellStart, unsigned *cellEnd,
                          unsigned numCells) {
   unsigned blocks = (numCells + 255) / 256;
-  if (blocks > 152u * 16u) blocks = 152u * 16u;
+  if (blocks > numSms() * 16u) blocks = numSms() * 16u;
   kCellTables<<<blocks, 256, 0, curStream()>>>(b.off, cellStart, cellEnd, numCells);
   return launchOk();
 }

@@ -353,7 +353,7 @@ fcdemDistanceMap *fcdemDistMapTorus(float majorRadius, float tubeRadius, int cel
   const int cells[3] = {cellsPerAxis, cellsPerAxis, cz};
   fcdemDistanceMap *m = fcdemDistMapCreate(nullptr, nullptr, vmin, vmax, cs, cells);
   if (!m) return nullptr;
-  kTorusMap<<<152 * 8, 256, 0, curStream()>>>(m->vert, cells[0] + 1, cells[1] + 1,
+  kTorusMap<<<numSms() * 8, 256, 0, curStream()>>>(m->vert, cells[0] + 1, cells[1] + 1,
                                               cells[2] + 1,
                                               make_float3(vmin[0], vmin[1], vmin[2]), cs,
                                               majorRadius, tubeRadius);
@@ -387,7 +387,7 @@ fcdemDistanceMap *fcdemDistMapRoundedBox(const float halfExtents[3], float round
   }
   fcdemDistanceMap *m = fcdemDistMapCreate(nullptr, nullptr, vmin, vmax, cs, cells);
   if (!m) return nullptr;
-  kRoundedBoxMap<<<152 * 8, 256, 0, curStream()>>>(
+  kRoundedBoxMap<<<numSms() * 8, 256, 0, curStream()>>>(
       m->vert, cells[0] + 1, cells[1] + 1, cells[2] + 1,
       make_float3(vmin[0], vmin[1], vmin[2]), cs,
       make_float3(halfExtents[0], halfExtents[1], halfExtents[2]), rounding);

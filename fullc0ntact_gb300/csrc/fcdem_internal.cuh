@@ -62,9 +62,18 @@ struct Context {
 
 // The context of the calling thread's current device (created on first use).
 Context &ctx();
-// The context of the current device if one has been created, else nullptr;
-// never creates one (creating one allocates its device status word).
-const Context *ctxIfCreated();
+// Copies the parameter block last given to setParameters on the current
+// device (read under the context lock) and returns true; false when there is
+// none.  Never creates a context (creating one allocates its status word).
+bool paramsIfSet(SimParams &out);
+// Multiprocessor count of the current device (queried once per device).
+unsigned numSms();
+// Look-back rounds a sort tile may make before it gives up
+// (fcdemSetSortWaitLimit; default kSortWaitRounds).
+unsigned sortWaitLimit();
+// The status word of the allocation-free sort on the current device, or
+// nullptr when that sort has not been set up there (fcdem_sort.cu).
+unsigned *noAllocStatusWord();
 // The stream this host thread issues work on (fcdemSetStream; default: the
 // legacy default stream, as the reference).
 cudaStream_t curStream();

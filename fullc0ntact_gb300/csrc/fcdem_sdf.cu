@@ -959,7 +959,7 @@ bool adamStep(fcdemSdfNet *net, float lr) {
 }
 
 // CTAs per SM that fit both the shared memory (227 KB) and the 512 TMEM
-// columns (H per CTA); the persistent grid is 152 times that.
+// columns (H per CTA); the persistent grid is the SM count times that.
 template <int H, int L>
 constexpr unsigned sdfCtasPerSm() {
   constexpr unsigned bySmem = (unsigned)((227u * 1024u) / (sizeof(SdfTileSmem<H, L>) + 1024u));
@@ -1003,7 +1003,7 @@ bool launchInfer(fcdemSdfNet *net, const float4 *pts, const int *shapes, unsigne
     residentOf[dev] = resident;
   }
   unsigned grid = (n + 128u * kInferTiles - 1) / (128u * kInferTiles);
-  if (grid > 152u * (unsigned)resident) grid = 152u * (unsigned)resident;
+  if (grid > numSms() * (unsigned)resident) grid = numSms() * (unsigned)resident;
   kSdfInfer<H, L><<<grid, threads, smem, curStream()>>>(sdfView(net), pts, shapes, n, d,
                                                         ctx().dStatus);
   return launchOk();
@@ -1015,7 +1015,7 @@ bool launchIntegrateSdf(fcdemSdfNet *net, float4 *pos, float4 *vel, float dt, un
                         const UmCount *count, TileHints hints) {
   const size_t smem = tileSmemBytes<H, L>();
   unsigned grid = (n + 127) / 128;
-  if (grid > 152u * sdfCtasPerSm<H, L>()) grid = 152u * sdfCtasPerSm<H, L>();
+  if (grid > numSms() * sdfCtasPerSm<H, L>()) grid = numSms() * sdfCtasPerSm<H, L>();
   if (count) {
     cudaFuncSetAttribute(kIntegrateSdf<H, L, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
@@ -1044,7 +1044,7 @@ bool launchBatchObstacle(fcdemSdfNet *net, const BatchScene *scenes, const unsig
     smem = tileSmemBytes<H, L>();
     cudaFuncSetAttribute(kBatchObstacle<H, L, kNet, kW>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (grid > 152u * sdfCtasPerSm<H, L>()) grid = 152u * sdfCtasPerSm<H, L>();
+    if (grid > numSms() * sdfCtasPerSm<H, L>()) grid = numSms() * sdfCtasPerSm<H, L>();
     v = sdfView(net);
   }
   kBatchObstacle<H, L, kNet, kW><<<grid, 128, smem, curStream()>>>(

@@ -1,5 +1,5 @@
 // fcdem_sort.cu -- stable LSD radix sort of (key, value) pairs: the stage
-// the reference hands to thrust::sort_by_key (particleSystem.cu:328-333).
+// the reference hands to thrust::sort_by_key (particleSystem.cu:265-270).
 //
 // One upsweep kernel builds the digit histograms of every pass in one read of
 // the keys; then each pass is a single "onesweep" kernel: a CTA takes the
@@ -9,9 +9,14 @@
 // thread reads kLookWindow predecessors per round), stages the tile in shared
 // memory in digit order and writes it out in runs.
 //
-// Every look-back spin is bounded: after kSpinLimit polls the CTA records
-// kStatusTimeout in the device status word and carries on, so a fault in the
-// protocol turns into an error the host reads, never into a hung GPU.
+// Every look-back wait is bounded: after a limit of rounds (kSortWaitRounds,
+// settable with fcdemSetSortWaitLimit) the CTA records kStatusTimeout in the
+// device status word and carries on with the part of its prefix it has
+// summed, so a fault in the protocol turns into an error the host reads,
+// never into a hung GPU.  Such a partial prefix is at most the true one, so
+// every write of the pass still lands inside [0, n) (the write-out also
+// guards it): the result is wrong, the memory outside the arrays untouched.
+#include <atomic>
 #include <mutex>
 
 #include "fcdem_internal.cuh"
@@ -28,8 +33,10 @@ constexpr int kMaxPasses = 4;
 constexpr unsigned kFlagAgg = 1u << 30;
 constexpr unsigned kFlagPrefix = 2u << 30;
 constexpr unsigned kValueMask = (1u << 30) - 1u;
-constexpr unsigned kSpinLimit = 1u << 22;
+constexpr unsigned kSortWaitRounds = 1u << 22;
 constexpr int kLookWindow = 8;  // look-back tiles read per round
+
+std::atomic<unsigned> g_sortWaitRounds{kSortWaitRounds};  // fcdemSetSortWaitLimit
 
 
 __device__ __forceinline__ unsigned lanemaskLt() {
@@ -158,7 +165,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
 kOnesweep(const unsigned *__restrict__ keysIn, const unsigned *__restrict__ valsIn,
           unsigned *__restrict__ keysOut, unsigned *__restrict__ valsOut,
           unsigned n, int shift, const unsigned *__restrict__ hist,
-          unsigned *lookback, unsigned *tileCounter, unsigned *status) {
+          unsigned *lookback, unsigned *tileCounter, unsigned *status, unsigned waitRounds) {
   static_assert(THREADS >= kRadix, "one thread per digit in the scan phases");
   constexpr int kWarps = THREADS / 32;
   constexpr int kTileKeys = THREADS * ITEMS;
@@ -227,11 +234,17 @@ kOnesweep(const unsigned *__restrict__ keysIn, const unsigned *__restrict__ vals
       // Look back kLookWindow tiles per round: their words are loaded
       // together (one latency for the window) and consumed nearest first,
       // adding aggregates until an inclusive prefix; a tile that has not
-      // published yet ends the round, and the next round starts there.
+      // published yet ends the round, and the next round starts there.  At
+      // most waitRounds rounds: then the wait has run out (kStatusTimeout)
+      // and excl keeps the aggregates summed so far.
       int t = (int)tile - 1;
-      unsigned spins = 0;
+      unsigned empty = 0;
       bool done = false;
-      while (!done) {
+      for (unsigned round = 0; !done; ++round) {
+        if (round >= waitRounds) {
+          atomicOr(status, (unsigned)kStatusTimeout);
+          break;
+        }
         unsigned w[kLookWindow];
 #pragma unroll
         for (int j = 0; j < kLookWindow; ++j)
@@ -248,13 +261,7 @@ kOnesweep(const unsigned *__restrict__ keysIn, const unsigned *__restrict__ vals
         }
         if (done) break;
         t -= used;  // t >= 0: tile 0 publishes a prefix, so the walk stops there
-        if (used == 0) {
-          if (++spins > kSpinLimit) {
-            atomicOr(status, (unsigned)kStatusTimeout);
-            break;
-          }
-          if (spins > 64) __nanosleep(64);
-        }
+        if (used == 0 && ++empty > 64) __nanosleep(64);
       }
       stVolatile(row + b, kFlagPrefix | ((excl + count) & kValueMask));
     }
@@ -304,7 +311,7 @@ struct PassConfig {
   int threads, items;
   size_t smem;
   void (*kernel)(const unsigned *, const unsigned *, unsigned *, unsigned *, unsigned, int,
-                 const unsigned *, unsigned *, unsigned *, unsigned *);
+                 const unsigned *, unsigned *, unsigned *, unsigned *, unsigned);
   int tile() const { return threads * items; }
 };
 
@@ -392,7 +399,7 @@ void radixSortPairs(Context &c, unsigned *keys, unsigned *vals, unsigned n,
 
   if (!cudaOk(cudaMemsetAsync(meta, 0, histBytes + lbBytes, st))) return;
   unsigned upBlocks = (n + kThreads * 16 - 1) / (kThreads * 16);
-  if (upBlocks > 152u * 4u) upBlocks = 152u * 4u;
+  if (upBlocks > numSms() * 4u) upBlocks = numSms() * 4u;
   kUpsweep<<<upBlocks, kThreads, 0, st>>>(keys, n, passes, bits, hist, c.dStatus);
   if (!launchOk()) return;
 
@@ -414,7 +421,7 @@ void radixSortPairs(Context &c, unsigned *keys, unsigned *vals, unsigned n,
     }
     pc.kernel<<<tiles, pc.threads, pc.smem, st>>>(
         srcK, srcV, dstK, dstV, n, p * kRadixBits, hist + p * kRadix,
-        lookback + (size_t)p * tiles * kRadix, counters + p, c.dStatus);
+        lookback + (size_t)p * tiles * kRadix, counters + p, c.dStatus, sortWaitLimit());
     if (!launchOk()) return;
     srcK = dstK;
     srcV = dstV;
@@ -429,14 +436,14 @@ void radixSortPairs(Context &c, unsigned *keys, unsigned *vals, unsigned n,
 // ---------------------------------------------------------------------------
 // sortParticles without allocation (fcdemSortParticlesNoAlloc).
 //
-// Some callers must not have the library allocate device memory: code that
-// records work into a CUDA graph (a cudaMalloc during stream capture breaks
-// the capture), hosts that own every byte of device memory through their own
-// pool and forbid hidden allocations, and loops running close to the memory
-// limit.  sortParticles grows its scratch with cudaMalloc on first use; this
-// variant uses a fixed scratch array in the library's static device memory
-// instead, sized for kNoAllocMaxParticles particles.  That array exists on
-// every GPU that loads the library, for the life of the process.
+// Some callers must not have the library allocate device memory: hosts that
+// own every byte of device memory through their own pool and forbid hidden
+// allocations, and loops running close to the memory limit, where a
+// cudaMalloc in the middle of a step can fail.  sortParticles grows its
+// scratch with cudaMalloc on first use; this variant uses a fixed scratch
+// array in the library's static device memory instead, sized for
+// kNoAllocMaxParticles particles.  That array exists on every GPU that loads
+// the library, for the life of the process.
 
 namespace {
 
@@ -451,15 +458,22 @@ constexpr size_t kNoAllocBytes =
 
 // The scratch itself.  In host code this name is only a host-side stand-in
 // for the device array, not a device address: the kernels get the address
-// that cudaGetSymbolAddress returns for the current device.
+// that cudaGetSymbolAddress returns for the current device.  Its last 256
+// bytes hold the sort's own status word (kStatus* bits), read and cleared
+// by fcdemGetLastError like the context's.
 static __device__ __align__(256) unsigned char g_noAllocScratch[kNoAllocBytes];
 
 constexpr int kNoAllocMaxDevices = 64;
 std::mutex g_noAllocMutex;
 unsigned char *g_noAllocPtr[kNoAllocMaxDevices] = {};
 
+unsigned *statusIn(unsigned char *scratch) {
+  return (unsigned *)(scratch + 4 * kNoAllocArr + kNoAllocHist + kNoAllocLookback);
+}
+
 // Device address of the scratch on the current device, looked up once per
-// device (with that device current) and cached; nullptr on failure.
+// device (with that device current) and cached, its status word cleared
+// then; nullptr on failure.
 unsigned char *noAllocScratch() {
   int dev = 0;
   if (!cudaOk(cudaGetDevice(&dev))) return nullptr;
@@ -473,6 +487,7 @@ unsigned char *noAllocScratch() {
       setError(FCDEM_ERR_CUDA);
       return nullptr;
     }
+    if (!cudaOk(cudaMemset(statusIn((unsigned char *)p), 0, sizeof(unsigned)))) return nullptr;
     g_noAllocPtr[dev] = (unsigned char *)p;
   }
   return g_noAllocPtr[dev];
@@ -480,7 +495,24 @@ unsigned char *noAllocScratch() {
 
 }  // namespace
 
+unsigned *noAllocStatusWord() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return nullptr;
+  std::lock_guard<std::mutex> lock(g_noAllocMutex);
+  return g_noAllocPtr[dev] ? statusIn(g_noAllocPtr[dev]) : nullptr;
+}
+
+unsigned sortWaitLimit() { return g_sortWaitRounds.load(std::memory_order_relaxed); }
+
 }  // namespace fcdem
+
+extern "C" void fcdemSetSortWaitLimit(int rounds) {
+  fcdem::g_sortWaitRounds.store(rounds < 0 ? fcdem::kSortWaitRounds : (unsigned)rounds);
+}
 
 extern "C" void fcdemSortParticlesNoAlloc(uint *dGridParticleHash, uint *dGridParticleIndex,
                                           uint numParticles) {
@@ -495,10 +527,10 @@ extern "C" void fcdemSortParticlesNoAlloc(uint *dGridParticleHash, uint *dGridPa
   unsigned char *s = noAllocScratch();
   if (!s) return;
   if (!prepareConfig(kPassConfigs[0])) return;  // 40 KB dynamic shared memory: fits the default
-  // Same key width as sortParticles; the existing context is used only if
-  // the caller already created one (setParameters), never created here.
-  const Context *c = ctxIfCreated();
-  int bits = (c && c->haveParams) ? keyBits(c->params.numCells) : 32;
+  // Same key width as sortParticles when setParameters has been called on
+  // this device (all 32 bits otherwise); no context is created here.
+  SimParams params;
+  const int bits = paramsIfSet(params) ? keyBits(params.numCells) : 32;
   const int passes = (bits + kRadixBits - 1) / kRadixBits;
   const unsigned tiles = (n + kTile - 1) / kTile;
   unsigned *keys = dGridParticleHash, *vals = dGridParticleIndex;
@@ -508,16 +540,17 @@ extern "C" void fcdemSortParticlesNoAlloc(uint *dGridParticleHash, uint *dGridPa
   unsigned *hist = (unsigned *)meta;
   unsigned *counters = hist + kMaxPasses * kRadix;
   unsigned *lookback = (unsigned *)(meta + kNoAllocHist);
-  unsigned *status = (c && c->dStatus) ? c->dStatus
-                                       : (unsigned *)(meta + kNoAllocHist + kNoAllocLookback);
+  unsigned *status = statusIn(s);
   cudaStream_t st = curStream();
   // The array keeps whatever the previous call left; the histograms, tile
-  // counters and look-back flags must start at zero.
+  // counters and look-back flags must start at zero.  (The status word is
+  // not cleared here: it holds the bits of earlier calls until
+  // fcdemGetLastError reads them.)
   if (!cudaOk(cudaMemsetAsync(meta, 0, kNoAllocHist + (size_t)passes * tiles * kRadix * 4,
                               st)))
     return;
   unsigned upBlocks = (n + kThreads * 16 - 1) / (kThreads * 16);
-  if (upBlocks > 152u * 4u) upBlocks = 152u * 4u;
+  if (upBlocks > numSms() * 4u) upBlocks = numSms() * 4u;
   kUpsweep<<<upBlocks, kThreads, 0, st>>>(keys, n, passes, bits, hist, status);
   if (!launchOk()) return;
   unsigned *srcK = keys, *srcV = vals;
@@ -536,7 +569,7 @@ extern "C" void fcdemSortParticlesNoAlloc(uint *dGridParticleHash, uint *dGridPa
     }
     kOnesweep<kThreads, kItems, 2><<<tiles, kThreads, onesweepSmem<kThreads, kItems>(), st>>>(
         srcK, srcV, dstK, dstV, n, p * kRadixBits, hist + p * kRadix,
-        lookback + (size_t)p * tiles * kRadix, counters + p, status);
+        lookback + (size_t)p * tiles * kRadix, counters + p, status, sortWaitLimit());
     if (!launchOk()) return;
     srcK = dstK;
     srcV = dstV;

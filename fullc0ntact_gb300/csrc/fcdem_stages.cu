@@ -1,6 +1,6 @@
 // fcdem_stages.cu -- integrate, hash, reorder and collide kernels and the
 // reference-named entry points that launch them
-// (particleSystem.cu:204-325, particles_kernel.cu:39-293).
+// (particleSystem.cu:141-262, particles_kernel.cu:39-293).
 #include "fcdem_dem.cuh"
 
 namespace fcdem {
@@ -9,7 +9,7 @@ constexpr unsigned kEmpty = 0xffffffffu;
 
 // ---------------------------------------------------------------------------
 // integrate (particles_kernel.cu:39-75; launched by thrust::for_each in
-// particleSystem.cu:204-216).  One thread per particle, 128-bit loads/stores.
+// particleSystem.cu:141-153).  One thread per particle, 128-bit loads/stores.
 __global__ void __launch_bounds__(256)
 kIntegrate(float4 *__restrict__ pos, float4 *__restrict__ vel, float dt,
            unsigned n, KParams kp) {
@@ -56,7 +56,7 @@ kIntegrateHash(float4 *__restrict__ pos, float4 *__restrict__ vel, float dt,
 }
 
 // ---------------------------------------------------------------------------
-// Fill (the cudaMemset of particleSystem.cu:261).  16-byte stores where the
+// Fill (the cudaMemset of particleSystem.cu:198).  16-byte stores where the
 // pointer allows, grid-stride.
 __global__ void __launch_bounds__(256)
 kFill(unsigned *__restrict__ p, size_t count, unsigned value) {
@@ -77,7 +77,7 @@ void fillU32(Context &, unsigned *p, size_t count, unsigned value) {
   if (count == 0) return;
   size_t work = (count + 3) / 4;
   unsigned blocks = (unsigned)((work + 255) / 256);
-  if (blocks > 152u * 16u) blocks = 152u * 16u;
+  if (blocks > numSms() * 16u) blocks = numSms() * 16u;
   if (blocks == 0) blocks = 1;
   kFill<<<blocks, 256, 0, curStream()>>>(p, count, value);
   launchOk();

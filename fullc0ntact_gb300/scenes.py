@@ -13,20 +13,39 @@ import math
 
 import numpy as np
 
-from . import _native
 from .params import SimParams, make_params
 
-_lib = _native.lib
 _f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
-_lib.fcdemSceneLattice.argtypes = [_f32p, _f32p, C.c_uint, C.c_float, C.c_float,
-                                   C.c_float, C.c_float, C.c_ulonglong]
-_lib.fcdemSceneLattice.restype = None
-_lib.fcdemScenePack.argtypes = [_f32p, _f32p, C.c_uint, _f32p, _f32p, C.c_float,
-                                C.c_float, C.c_float, C.c_float, C.c_ulonglong, C.c_uint]
-_lib.fcdemScenePack.restype = C.c_uint
-_lib.fcdemScenePackRadii.argtypes = [_f32p, _f32p, C.c_uint, _f32p, _f32p, _f32p, C.c_float,
-                                     C.c_ulonglong, C.c_uint]
-_lib.fcdemScenePackRadii.restype = C.c_uint
+_GEN = None
+
+
+def _declare(lib):
+    lib.fcdemSceneLattice.argtypes = [_f32p, _f32p, C.c_uint, C.c_float, C.c_float,
+                                      C.c_float, C.c_float, C.c_ulonglong]
+    lib.fcdemSceneLattice.restype = None
+    lib.fcdemScenePack.argtypes = [_f32p, _f32p, C.c_uint, _f32p, _f32p, C.c_float,
+                                   C.c_float, C.c_float, C.c_float, C.c_ulonglong, C.c_uint]
+    lib.fcdemScenePack.restype = C.c_uint
+    lib.fcdemScenePackRadii.argtypes = [_f32p, _f32p, C.c_uint, _f32p, _f32p, _f32p,
+                                        C.c_float, C.c_ulonglong, C.c_uint]
+    lib.fcdemScenePackRadii.restype = C.c_uint
+    return lib
+
+
+def use_generator(lib) -> None:
+    """Builds scenes with the generator entry points of `lib` (a ctypes
+    library exporting fcdemSceneLattice / fcdemScenePack /
+    fcdemScenePackRadii) instead of libfcdem.so's."""
+    global _GEN
+    _GEN = _declare(lib)
+
+
+def _lib():
+    global _GEN
+    if _GEN is None:
+        from . import _native
+        _GEN = _declare(_native.lib)
+    return _GEN
 
 
 def lattice(n: int, radius: float, jitter: float, vel_range: float, seed: int,
@@ -34,7 +53,7 @@ def lattice(n: int, radius: float, jitter: float, vel_range: float, seed: int,
     pos = np.zeros((n, 4), np.float32)
     vel = np.zeros((n, 4), np.float32)
     sp = 2.0 * radius if spacing is None else spacing
-    _lib.fcdemSceneLattice(pos, vel, n, radius, sp, jitter, vel_range, seed)
+    _lib().fcdemSceneLattice(pos, vel, n, radius, sp, jitter, vel_range, seed)
     return pos, vel
 
 
@@ -42,7 +61,7 @@ def pack(n: int, box_min, box_max, r_median: float, sigma: float, r_max: float,
          vel_range: float, seed: int, max_attempts: int = 20000):
     pos = np.zeros((n, 4), np.float32)
     vel = np.zeros((n, 4), np.float32)
-    placed = _lib.fcdemScenePack(pos, vel, n, np.asarray(box_min, np.float32),
+    placed = _lib().fcdemScenePack(pos, vel, n, np.asarray(box_min, np.float32),
                                  np.asarray(box_max, np.float32), r_median, sigma,
                                  r_max, vel_range, seed, max_attempts)
     if placed != n:
@@ -139,7 +158,7 @@ def pack_radii(radii: np.ndarray, box_min, box_max, vel_range: float, seed: int,
     n = radii.shape[0]
     pos = np.zeros((n, 4), np.float32)
     vel = np.zeros((n, 4), np.float32)
-    placed = _lib.fcdemScenePackRadii(pos, vel, n, np.ascontiguousarray(radii, np.float32),
+    placed = _lib().fcdemScenePackRadii(pos, vel, n, np.ascontiguousarray(radii, np.float32),
                                       np.asarray(box_min, np.float32),
                                       np.asarray(box_max, np.float32), vel_range, seed,
                                       max_attempts)

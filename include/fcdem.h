@@ -4,7 +4,7 @@
  * The first block of entry points has exactly the names, argument lists and
  * meaning of FullC0ntact's particle-system C interface
  * (cuda_addon/particleSystem.cuh:12-63, implemented in
- * cuda_addon/particleSystem.cu:99-335), so host code written against that
+ * cuda_addon/particleSystem.cu:36-272), so host code written against that
  * header links against libfcdem.so unchanged.  Pointers are DEVICE pointers;
  * positions and velocities are float4 per particle (x, y, z, w), 16 bytes.
  *
@@ -64,24 +64,24 @@ struct cudaGraphicsResource;
 /* ---------------------------------------------------------------------- */
 /* Support calls (particleSystem.cuh:14-26). */
 
-/* particleSystem.cu:102-116: selects a device.  "-device=N" in argv picks N,
+/* particleSystem.cu:39-63: selects a device.  "-device=N" in argv picks N,
  * otherwise device 0 (the GB300 build targets one GPU per process). */
 void cudaInit(int argc, char **argv);
-/* particleSystem.cu:128-131 (the implementation takes size_t; the reference
+/* particleSystem.cu:65-68 (the implementation takes size_t; the reference
  * header says int). */
 void allocateArray(void **devPtr, size_t size);
-/* particleSystem.cu:133-136 */
+/* particleSystem.cu:70-73 */
 void freeArray(void *devPtr);
-/* particleSystem.cu:138-141: waits for all work issued by this library. */
+/* particleSystem.cu:75-78: waits for all work issued by this library. */
 void threadSync(void);
-/* particleSystem.cu:174-184: a non-null GL resource records
+/* particleSystem.cu:111-121: a non-null GL resource records
  * FCDEM_ERR_UNSUPPORTED and copies nothing. */
 void copyArrayFromDevice(void *host, const void *device,
                          struct cudaGraphicsResource **cuda_vbo_resource,
                          int size);
-/* particleSystem.cu:143-146 */
+/* particleSystem.cu:80-83 */
 void copyArrayToDevice(void *device, const void *host, int offset, int size);
-/* particleSystem.cu:148-172: OpenGL interop.  Stubs: record
+/* particleSystem.cu:85-109: OpenGL interop.  Stubs: record
  * FCDEM_ERR_UNSUPPORTED; map returns NULL. */
 void registerGLBufferObject(uint vbo, struct cudaGraphicsResource **cuda_vbo_resource);
 void unregisterGLBufferObject(struct cudaGraphicsResource *cuda_vbo_resource);
@@ -91,52 +91,58 @@ void unmapGLBufferObject(struct cudaGraphicsResource *cuda_vbo_resource);
 /* ---------------------------------------------------------------------- */
 /* The five stages (particleSystem.cuh:29-61). */
 
-/* particleSystem.cu:186-190: copies the parameter block; every later launch
+/* particleSystem.cu:123-127: copies the parameter block; every later launch
  * on this device uses this copy until the next call. */
 void setParameters(SimParams *hostParams);
 
-/* particleSystem.cu:204-216 + particles_kernel.cu:39-75:
+/* particleSystem.cu:141-153 + particles_kernel.cu:39-75:
  * v += g*dt; v *= globalDamping; p += v*dt; clamp to [-1+r, 1-r] per axis
  * with v_axis *= boundaryDamping on contact.  In place. */
 void integrateSystem(float *pos, float *vel, float deltaTime, uint numParticles);
 
-/* particleSystem.cu:228-244 + particles_kernel.cu:78-115:
+/* particleSystem.cu:165-181 + particles_kernel.cu:78-115:
  * hash[i] = wrapped linear cell id of pos[i], index[i] = i. */
 void calcHash(uint *gridParticleHash, uint *gridParticleIndex, float *pos,
               int numParticles);
 
-/* particleSystem.cu:328-333: stable ascending sort of (hash, index) in place.
+/* particleSystem.cu:265-270: stable ascending sort of (hash, index) in place.
  * Keys are expected below 2^ceil(log2(numCells)) of the current parameters;
  * a larger key records FCDEM_ERR_KEY_RANGE. */
 void sortParticles(uint *dGridParticleHash, uint *dGridParticleIndex,
                    uint numParticles);
 
 /* No counterpart in the reference.  The same sort as sortParticles, for
- * callers that must not have the library allocate device memory: code being
- * recorded into a CUDA graph (a cudaMalloc during stream capture invalidates
- * the capture), hosts whose own pool owns all device memory, and loops run
- * near the memory limit.  sortParticles allocates its scratch on first use;
- * this entry point allocates nothing and uses a fixed ~17 MB scratch array in
- * the library's static device memory, present on every GPU that loads the
- * library until the process exits.
+ * callers that must not have the library allocate device memory: hosts whose
+ * own pool owns all device memory and forbid hidden allocations, and loops
+ * run near the memory limit, where an allocation in the middle of a step can
+ * fail.  sortParticles allocates its scratch on first use; this entry point
+ * allocates nothing and uses a fixed ~17 MB scratch array in the library's
+ * static device memory, present on every GPU that loads the library until
+ * the process exits.
  *   - At most 1,048,576 particles; more records FCDEM_ERR_INVALID_VALUE and
  *     leaves the arrays untouched.
+ *   - Key width: that of the numCells last given to setParameters on this
+ *     device, all 32 bits before any setParameters.
  *   - Its first call on a device looks up that array's device address (with
- *     the device current); make that first call before any stream capture.
+ *     the device current) and clears the sort's status word in it; make that
+ *     first call before any stream capture.
  *   - Every call shares the one array: calls that overlap on the GPU (other
  *     streams, other host threads) race and corrupt each other's results.
- *     Issue them in order on one stream. */
+ *     Issue them in order on one stream.
+ *   - Device-side errors (a key above the key width, a bounded wait that ran
+ *     out) are kept in that array's status word until fcdemGetLastError
+ *     reads them. */
 void fcdemSortParticlesNoAlloc(uint *dGridParticleHash, uint *dGridParticleIndex,
                                uint numParticles);
 
-/* particleSystem.cu:246-285 + particles_kernel.cu:119-182 */
+/* particleSystem.cu:183-222 + particles_kernel.cu:119-182 */
 void reorderDataAndFindCellStart(uint *cellStart, uint *cellEnd,
                                  float *sortedPos, float *sortedVel,
                                  uint *gridParticleHash, uint *gridParticleIndex,
                                  float *oldPos, float *oldVel,
                                  uint numParticles, uint numCells);
 
-/* particleSystem.cu:287-325 + particles_kernel.cu:185-293 */
+/* particleSystem.cu:224-262 + particles_kernel.cu:185-293 */
 void collide(float *newVel, float *sortedPos, float *sortedVel,
              uint *gridParticleIndex, uint *cellStart, uint *cellEnd,
              uint numParticles, uint numCells);
@@ -218,6 +224,13 @@ void fcdemUpdate(float *pos, float *vel, float *sortedPos, float *sortedVel,
 /* Collide kernel selection: -1 (default) automatic, 0 the global-read
  * kernel, 1 the shared-memory tiled kernel.  Both give identical results. */
 void fcdemSetCollidePath(int path);
+
+/* Test hook: the number of look-back rounds a tile of the radix sort
+ * (sortParticles, fcdemSortParticlesNoAlloc) may wait for its predecessors
+ * before it gives up, records FCDEM_ERR_DEVICE_TIMEOUT and finishes with the
+ * prefix it has (a wrong order, every write still inside the arrays).
+ * 0: no waiting at all; negative: the default, 2^22 rounds. */
+void fcdemSetSortWaitLimit(int rounds);
 
 /* Sort tuning.  The counting passes of the sort come in several block
  * shapes (threads x keys per thread); results are identical.

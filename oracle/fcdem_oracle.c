@@ -503,3 +503,126 @@ void orc_integrate_distmap(const SimParams *P, const orc_distmap *m,
     v4[0] = v[0]; v4[1] = v[1]; v4[2] = v[2]; v4[3] = p4[3];
   }
 }
+
+/* ---------------------------------------------------------------------- */
+/* Batched scenes.  Each scene of a batch is stepped as one ParticleSystem
+ * with its own parameters and its own box [lo, hi] (the reference's box is
+ * [-1, 1]^3).  Below, the reference's GPU arithmetic is restated as nvcc
+ * builds it: `vel += gravity * deltaTime` and `pos += vel * deltaTime` of
+ * particles_kernel.cu:55-59 and particledem_um.cu:625-630 are contracted
+ * into fused multiply-adds (fmaf, correctly rounded in C99 as on the GPU). */
+
+/* particles_kernel.cu:39-75 with the faces of the box [lo, hi], in the
+ * reference's order (+x, -x, +y, +z, -z, -y). */
+static inline void box_faces(float lo[3], float hi[3], float r, float bd,
+                             float p[3], float v[3]) {
+  if (p[0] > hi[0] - r) { p[0] = hi[0] - r; v[0] = v[0] * bd; }
+  if (p[0] < lo[0] + r) { p[0] = lo[0] + r; v[0] = v[0] * bd; }
+  if (p[1] > hi[1] - r) { p[1] = hi[1] - r; v[1] = v[1] * bd; }
+  if (p[2] > hi[2] - r) { p[2] = hi[2] - r; v[2] = v[2] * bd; }
+  if (p[2] < lo[2] + r) { p[2] = lo[2] + r; v[2] = v[2] * bd; }
+  if (p[1] < lo[1] + r) { p[1] = lo[1] + r; v[1] = v[1] * bd; }
+}
+
+void orc_integrate_box(const SimParams *P, const float lo[3], const float hi[3],
+                       float *pos, float *vel, float dt, unsigned n,
+                       int radius_from_w) {
+  float l[3] = {lo[0], lo[1], lo[2]}, h[3] = {hi[0], hi[1], hi[2]};
+  for (unsigned i = 0; i < n; ++i) {
+    float *p4 = pos + 4 * (size_t)i, *v4 = vel + 4 * (size_t)i;
+    float p[3] = {p4[0], p4[1], p4[2]}, v[3] = {v4[0], v4[1], v4[2]};
+    float r = radius_from_w ? p4[3] : P->particleRadius;
+    for (int k = 0; k < 3; ++k) v[k] = fmaf(P->gravity[k], dt, v[k]);
+    for (int k = 0; k < 3; ++k) v[k] = v[k] * P->globalDamping;
+    for (int k = 0; k < 3; ++k) p[k] = fmaf(v[k], dt, p[k]);
+    box_faces(l, h, r, P->boundaryDamping, p, v);
+    p4[0] = p[0]; p4[1] = p[1]; p4[2] = p[2];
+    v4[0] = v[0]; v4[1] = v[1]; v4[2] = v[2];
+  }
+}
+
+/* distancemap.cuh:154-191 as the GPU build evaluates it: the distance as in
+ * orc_distmap_query (its double products are not contracted), each
+ * contact-point blend `a * w0 + b * w1` of trilinearInterpolateCP
+ * (distancemap.cuh:254-279) as fmaf(a, w0, b * w1). */
+static void distmap_query_fused(const orc_distmap *m, const float q[3],
+                                float *dist, float cp[3]) {
+  orc_distmap_query(m, q, dist, cp);
+  if (*dist == 5.0f &&
+      !(m->vmin[0] <= q[0] && q[0] <= m->vmax[0] && m->vmin[1] <= q[1] &&
+        q[1] <= m->vmax[1] && m->vmin[2] <= q[2] && q[2] <= m->vmax[2]))
+    return;
+  float inv = (float)(1.0 / (double)m->cellSize);
+  int c[3];
+  for (int k = 0; k < 3; ++k)
+    c[k] = clampi((int)(fabsf(q[k] - m->vmin[k]) * inv), 0, m->cells[k] - 1);
+  int ix = m->cells[0] + 1;
+  int islice = (m->cells[0] + 1) * (m->cells[1] + 1);
+  int b = c[2] * islice + c[1] * ix + c[0];
+  int idx[8] = {b, b + 1, b + ix + 1, b + ix, b + islice, b + islice + 1,
+                b + ix + islice + 1, b + ix + islice};
+  float x0 = vcoord(m->vmin[0], c[0], m->cellSize);
+  float x1 = vcoord(m->vmin[0], c[0] + 1, m->cellSize);
+  float y0 = vcoord(m->vmin[1], c[1], m->cellSize);
+  float y1 = vcoord(m->vmin[1], c[1] + 1, m->cellSize);
+  float z0 = vcoord(m->vmin[2], c[2], m->cellSize);
+  float z1 = vcoord(m->vmin[2], c[2] + 1, m->cellSize);
+  float xd = (q[0] - x0) / (x1 - x0);
+  float yd = (q[1] - y0) / (y1 - y0);
+  float zd = (q[2] - z0) / (z1 - z0);
+  float fwx = (float)(1.0 - (double)xd), fwy = (float)(1.0 - (double)yd);
+  float fwz = (float)(1.0 - (double)zd);
+  const float *C = m->contactPoints;
+  for (int k = 0; k < 3; ++k) {
+    float a00 = fmaf(C[3 * idx[0] + k], fwx, C[3 * idx[1] + k] * xd);
+    float a10 = fmaf(C[3 * idx[3] + k], fwx, C[3 * idx[2] + k] * xd);
+    float a01 = fmaf(C[3 * idx[4] + k], fwx, C[3 * idx[5] + k] * xd);
+    float a11 = fmaf(C[3 * idx[7] + k], fwx, C[3 * idx[6] + k] * xd);
+    float a0 = fmaf(a00, fwy, a10 * yd);
+    float a1 = fmaf(a01, fwy, a11 * yd);
+    cp[k] = fmaf(a0, fwz, a1 * zd);
+  }
+}
+
+void orc_batch_obstacle_integrate(const SimParams *P, const float lo[3],
+                                  const float hi[3], const orc_distmap *m,
+                                  float *pos, float *vel, float dt, unsigned n,
+                                  int radius_from_w, unsigned *contacts) {
+  float l[3] = {lo[0], lo[1], lo[2]}, h[3] = {hi[0], hi[1], hi[2]};
+  unsigned nc = 0;
+  for (unsigned i = 0; i < n; ++i) {
+    float *p4 = pos + 4 * (size_t)i, *v4 = vel + 4 * (size_t)i;
+    float p[3] = {p4[0], p4[1], p4[2]}, v[3] = {v4[0], v4[1], v4[2]};
+    float r = radius_from_w ? p4[3] : P->particleRadius;
+    float bd = P->boundaryDamping;
+    /* particledem_um.cu:625-630 */
+    for (int k = 0; k < 3; ++k) v[k] = fmaf(P->gravity[k], dt, v[k]);
+    for (int k = 0; k < 3; ++k) v[k] = v[k] * P->globalDamping;
+    for (int k = 0; k < 3; ++k) p[k] = fmaf(v[k], dt, p[k]);
+    if (m) {
+      /* checkDistMap, boundaries.cuh:38-63 */
+      float dist = 0.0f, cp[3] = {0.0f, 0.0f, 0.0f};
+      distmap_query_fused(m, p, &dist, cp);
+      if (dist < r) {
+        float n0[3] = {p[0] - cp[0], p[1] - cp[1], p[2] - cp[2]};
+        /* normalize = v * rsqrtf(dot(v, v)); rsqrtf restated as 1/sqrtf
+         * (the GPU's rsqrtf is within 2 ulp of it) */
+        float dd = fmaf(n0[0], n0[0], fmaf(n0[1], n0[1], n0[2] * n0[2]));
+        float invLen = 1.0f / sqrtf(dd);
+        float nn[3] = {n0[0] * invLen, n0[1] * invLen, n0[2] * invLen};
+        float pen = r - dist;
+        float extra = (float)(0.1 * (double)r);
+        for (int k = 0; k < 3; ++k) p[k] = fmaf(nn[k], pen, p[k]);
+        for (int k = 0; k < 3; ++k) p[k] = fmaf(nn[k], extra, p[k]);
+        v[0] = v[0] * (0.5f * bd);
+        v[1] = v[1] * (0.5f * bd);
+        v[2] = v[2] * (0.7f * bd);
+        ++nc;
+      }
+    }
+    box_faces(l, h, r, bd, p, v);
+    p4[0] = p[0]; p4[1] = p[1]; p4[2] = p[2];
+    v4[0] = v[0]; v4[1] = v[1]; v4[2] = v[2];
+  }
+  if (contacts) *contacts = nc;
+}

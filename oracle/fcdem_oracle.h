@@ -28,11 +28,11 @@ void orc_integrate(const SimParams *P, float *pos, float *vel, float dt,
 void orc_calc_hash(const SimParams *P, unsigned *hash, unsigned *index,
                    const float *pos, unsigned n);
 
-/* particleSystem.cu:328-333 (thrust::sort_by_key): stable ascending sort of
+/* particleSystem.cu:265-270 (thrust::sort_by_key): stable ascending sort of
  * (key, value) pairs, restated as an LSD counting sort over 8-bit digits. */
 void orc_sort_pairs(unsigned *keys, unsigned *vals, unsigned n);
 
-/* particleSystem.cu:246-285 + particles_kernel.cu:119-182.  cellStart is set
+/* particleSystem.cu:183-222 + particles_kernel.cu:119-182.  cellStart is set
  * to 0xffffffff first; cellEnd of empty cells is not touched. */
 void orc_reorder(unsigned *cellStart, unsigned *cellEnd, float *sortedPos,
                  float *sortedVel, const unsigned *hash, const unsigned *index,
@@ -96,6 +96,28 @@ void orc_check_distmap(const orc_distmap *m, float radius,
 void orc_integrate_distmap(const SimParams *P, const orc_distmap *m,
                            float *pos, float *vel, float dt, unsigned n,
                            int radius_from_w);
+
+/* ---------------------------------------------------------------------- */
+/* Batched scenes: one scene of a batch is one ParticleSystem with its own
+ * parameters and its own box [lo, hi] instead of [-1, 1]^3.  The velocity
+ * and position updates are fused multiply-adds, as nvcc builds the
+ * reference's integrate (particles_kernel.cu:55-59, particledem_um.cu:625-630). */
+
+/* particles_kernel.cu:39-75 with the faces of [lo, hi] in the reference's
+ * order (+x, -x, +y, +z, -z, -y). */
+void orc_integrate_box(const SimParams *P, const float lo[3], const float hi[3],
+                       float *pos, float *vel, float dt, unsigned n,
+                       int radius_from_w);
+
+/* The integrate of a batched scene with an obstacle: the velocity and
+ * position update of particledem_um.cu:604-638, checkDistMap
+ * (boundaries.cuh:38-63) against the map m (NULL: no obstacle), then the
+ * faces of [lo, hi].  *contacts (optional) receives the number of particles
+ * the map pushed out. */
+void orc_batch_obstacle_integrate(const SimParams *P, const float lo[3],
+                                  const float hi[3], const orc_distmap *m,
+                                  float *pos, float *vel, float dt, unsigned n,
+                                  int radius_from_w, unsigned *contacts);
 
 #ifdef __cplusplus
 }

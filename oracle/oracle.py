@@ -105,12 +105,25 @@ def lib():
         L.orc_distmap_query.argtypes = [C.POINTER(DistMap), _f32p, C.POINTER(C.c_float), _f32p]
         L.orc_integrate_distmap.argtypes = [P, C.POINTER(DistMap), _f32p, _f32p,
                                             C.c_float, C.c_uint, C.c_int]
+        L.orc_integrate_box.argtypes = [P, _f32p, _f32p, _f32p, _f32p, C.c_float, C.c_uint,
+                                        C.c_int]
+        L.orc_batch_obstacle_integrate.argtypes = [P, _f32p, _f32p, C.c_void_p, _f32p, _f32p,
+                                                   C.c_float, C.c_uint, C.c_int,
+                                                   C.POINTER(C.c_uint)]
         for f in ("orc_integrate", "orc_calc_hash", "orc_sort_pairs", "orc_reorder",
                   "orc_collide", "orc_collide_f64", "orc_update", "orc_distmap_query",
-                  "orc_integrate_distmap"):
+                  "orc_integrate_distmap", "orc_integrate_box",
+                  "orc_batch_obstacle_integrate"):
             getattr(L, f).restype = None
         L._typed = True
     return L
+
+
+def scenegen():
+    """The seeded scene generators built from the product's generator source
+    as a host-only library (_build/libscenegen.so), for code that must build
+    the benchmark's scenes without loading the GPU library."""
+    return _load("scenegen", os.path.join(BUILD, "libscenegen.so"))
 
 
 def ref_host_available() -> bool:
@@ -160,6 +173,20 @@ def ref_gpu():
         rc = L.fcrefgpu_load(cubin.encode())
         if rc != 0:
             raise RuntimeError(f"loading the reference cubin failed (code {rc})")
+        L._typed = True
+    return L
+
+
+def ref_thrust_sort():
+    """thrust::sort_by_key on device arrays, as the reference's sortParticles
+    issues it (particleSystem.cu:265-270); None when not built."""
+    path = os.path.join(BUILD, "libfcref_thrust_sort.so")
+    if not os.path.exists(path):
+        return None
+    L = _load("ref_thrust_sort", path)
+    if not getattr(L, "_typed", False):
+        L.fcrefgpu_sort_by_key.argtypes = [C.c_void_p, C.c_void_p, C.c_uint]
+        L.fcrefgpu_sort_by_key.restype = C.c_int
         L._typed = True
     return L
 
@@ -304,3 +331,56 @@ def distmap_query(m, q):
 def integrate_distmap(P, m, pos, vel, dt, radius_from_w=False):
     lib().orc_integrate_distmap(C.byref(P), C.byref(m), pos, vel, dt, pos.shape[0],
                                 int(radius_from_w))
+
+
+# ---------------------------------------------------------------------------
+# batched scenes: each scene of a batch is one ParticleSystem in its own box
+
+
+def _box(scene):
+    lo = np.ascontiguousarray(scene.get("box_lo", (-1.0, -1.0, -1.0)), np.float32)
+    hi = np.ascontiguousarray(scene.get("box_hi", (1.0, 1.0, 1.0)), np.float32)
+    return lo, hi
+
+
+def integrate_box(P, lo, hi, pos, vel, dt, radius_from_w=False):
+    lib().orc_integrate_box(C.byref(P), np.ascontiguousarray(lo, np.float32),
+                            np.ascontiguousarray(hi, np.float32), pos, vel, dt,
+                            pos.shape[0], int(radius_from_w))
+
+
+def batch_obstacle_integrate(P, lo, hi, m, pos, vel, dt, radius_from_w=False):
+    """The obstacle integrate of a batched scene; m is a DistMap (or None).
+    Returns the number of particles the map pushed out."""
+    nc = C.c_uint(0)
+    lib().orc_batch_obstacle_integrate(C.byref(P), np.ascontiguousarray(lo, np.float32),
+                                       np.ascontiguousarray(hi, np.float32),
+                                       C.cast(C.pointer(m), C.c_void_p) if m is not None
+                                       else None, pos, vel, dt, pos.shape[0],
+                                       int(radius_from_w), C.byref(nc))
+    return int(nc.value)
+
+
+def batch_scene_step(scene, m=None, obstacle=False, nthreads=None, pos=None, vel=None):
+    """One update of one batched scene on copies of (pos, vel) (default: the
+    scene's): the integrate in the scene's box (with the obstacle contact of
+    map m when `obstacle`), calcHash, sortParticles, reorder, collide with
+    the collider sphere (the batch step always applies it).  Returns every
+    intermediate, as step_stages."""
+    P = SimParams.from_buffer_copy(bytes(scene["params"]))
+    w = bool(scene.get("radius_from_w", False))
+    pos = (scene["pos"] if pos is None else pos).copy()
+    vel = (scene["vel"] if vel is None else vel).copy()
+    lo, hi = _box(scene)
+    contacts = 0
+    if obstacle:
+        contacts = batch_obstacle_integrate(P, lo, hi, m, pos, vel, scene["dt"], w)
+    else:
+        integrate_box(P, lo, hi, pos, vel, scene["dt"], w)
+    h, x = calc_hash(P, pos)
+    hs, xs = sort_pairs(h, x)
+    cs, ce, sp, sv = reorder(hs, xs, pos, vel, P.numCells)
+    nv = collide(P, sp, sv, xs, cs, ce, w, True, nthreads)
+    return dict(pos=pos, vel_in=vel, hash=h, index=x, hash_sorted=hs, index_sorted=xs,
+                cellStart=cs, cellEnd=ce, sortedPos=sp, sortedVel=sv, newVel=nv,
+                map_contacts=contacts)

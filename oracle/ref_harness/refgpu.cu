@@ -7,7 +7,7 @@
  * __constant__ block `params` are used as the reference defines them; the one
  * wrapper below applies the reference's integrate_functor to element i, which
  * is what thrust::for_each over zip(pos4, vel4) does
- * (particleSystem.cu:204-216).
+ * (particleSystem.cu:141-153).
  */
 #include <thrust/tuple.h>
 #include "particles_kernel.cu"

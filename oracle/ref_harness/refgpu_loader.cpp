@@ -2,11 +2,11 @@
  * refgpu_loader.cpp -- TEST INFRASTRUCTURE.  Loads
  * oracle/_ref/fcref_kernels.cubin (the reference's own kernels, see
  * refgpu.cu) with the CUDA driver API and launches them with the launch glue
- * of cuda_addon/particleSystem.cu:192-333 restated: 256 threads per block for
+ * of cuda_addon/particleSystem.cu:135-270 restated: 256 threads per block for
  * calcHash and reorder, 64 for collide, a 0xff memset of cellStart before
  * the reorder, (blockDim + 1) * 4 bytes of dynamic shared memory for it, and
  * the parameter block copied into the module's __constant__ `params`
- * (particleSystem.cu:186-190).  All pointers are device pointers; launches go
+ * (particleSystem.cu:123-127).  All pointers are device pointers; launches go
  * to the given stream (0 = legacy default stream).
  */
 #include <cuda.h>

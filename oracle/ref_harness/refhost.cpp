@@ -2,7 +2,7 @@
  * refhost.cpp -- TEST INFRASTRUCTURE.  Builds the reference's own kernel
  * file (cuda_addon/particles_kernel.cu, included from the reference tree at
  * build time, never copied) as host code, and drives it with the launch glue
- * of cuda_addon/particleSystem.cu:192-333 restated: 256 threads per block for
+ * of cuda_addon/particleSystem.cu:135-270 restated: 256 threads per block for
  * calcHash and reorder, 64 for collide, cellStart memset to 0xff before the
  * reorder, a stable sort of (hash, index) for sortParticles.
  *
@@ -33,7 +33,7 @@ void fcref_setParameters(const void *hostParams) {
   std::memcpy(&params, hostParams, sizeof(SimParams));
 }
 
-/* particleSystem.cu:204-216: thrust::for_each over zip(pos4, vel4). */
+/* particleSystem.cu:141-153: thrust::for_each over zip(pos4, vel4). */
 void fcref_integrateSystem(float *pos, float *vel, float deltaTime,
                            uint numParticles) {
   float4 *p = (float4 *)pos, *v = (float4 *)vel;

@@ -114,3 +114,40 @@ def test_autotune_picks_a_configuration():
     rk, rv = _sort_cpu(keys, vals)
     np.testing.assert_array_equal(gv, rv)
     dem.lib.fcdemSetSortConfig(200_000, -1)
+
+
+def test_lookback_wait_that_runs_out_is_reported_and_recovers():
+    """The look-back wait of the radix sort is bounded.  With a limit of zero
+    rounds every tile after the first gives up at once: the sort records
+    FCDEM_ERR_DEVICE_TIMEOUT, and its writes stay inside the arrays (a
+    partial prefix is at most the true one; the guard words around the
+    arrays are untouched).  With the default limit restored the next sort is
+    correct."""
+    from fullc0ntact_gb300 import dem
+    from fullc0ntact_gb300.params import make_params
+    lib = dem.lib
+    n, cells, pad = 300_000, 2 ** 24, 4096  # 74 tiles of 4096 keys, 3 passes
+    rng = np.random.default_rng(77)
+    keys = rng.integers(0, cells, n).astype(np.uint32)
+    vals = np.arange(n, dtype=np.uint32)
+    P = make_params(n, (256, 256, 256), 0.01)
+    dem.set_parameters(P)
+    guard = -123456789
+    kb = torch.full((n + 2 * pad,), guard, dtype=torch.int32, device="cuda")
+    vb = torch.full((n + 2 * pad,), guard, dtype=torch.int32, device="cuda")
+    kb[pad:pad + n] = torch.from_numpy(keys.view(np.int32)).cuda()
+    vb[pad:pad + n] = torch.from_numpy(vals.view(np.int32)).cuda()
+    assert lib.fcdemGetLastError() == 0
+    try:
+        lib.fcdemSetSortWaitLimit(0)
+        lib.sortParticles(kb.data_ptr() + 4 * pad, vb.data_ptr() + 4 * pad, n)
+        code = lib.fcdemGetLastError()
+    finally:
+        lib.fcdemSetSortWaitLimit(-1)
+    assert code == 5, code  # FCDEM_ERR_DEVICE_TIMEOUT
+    for b in (kb, vb):
+        assert bool((b[:pad] == guard).all()) and bool((b[pad + n:] == guard).all())
+    k, v = _sort_gpu(keys, vals, cells)  # the context still works
+    rk, rv = _sort_cpu(keys, vals)
+    np.testing.assert_array_equal(k, rk)
+    np.testing.assert_array_equal(v, rv)
