@@ -28,7 +28,7 @@ P = C.POINTER(SimParams)
 _SIGS = {
     # reference names (cuda_addon/particleSystem.cuh:12-63)
     "cudaInit": (None, [C.c_int, C.POINTER(C.c_char_p)]),
-    "allocateArray": (None, [C.POINTER(vp), C.c_size_t]),
+    "allocateArray": (None, [C.POINTER(vp), C.c_int]),
     "freeArray": (None, [vp]),
     "threadSync": (None, []),
     "copyArrayFromDevice": (None, [vp, vp, vp, C.c_int]),

@@ -26,6 +26,8 @@ SOURCES = [
     "fcdem_sdf.cu",
     "fcdem_host.cpp",
     "fcdem_scenes.cpp",
+    "fcdem_i3d.cu",
+    "fcdem_i3d_integrate.cpp",
 ]
 # per-file host-compiler flags (the scene generators round every a*b+c
 # twice, as the reference arm's build of the same file does)

@@ -188,9 +188,9 @@ void cudaInit(int argc, char **argv) {
   cudaOk(cudaSetDevice(dev));
 }
 
-void allocateArray(void **devPtr, size_t size) {
-  if (!devPtr) { setError(FCDEM_ERR_INVALID_VALUE); return; }
-  if (cudaMalloc(devPtr, size) != cudaSuccess) {
+void allocateArray(void **devPtr, int size) {
+  if (!devPtr || size < 0) { setError(FCDEM_ERR_INVALID_VALUE); return; }
+  if (cudaMalloc(devPtr, (size_t)size) != cudaSuccess) {
     cudaGetLastError();
     *devPtr = nullptr;
     setError(FCDEM_ERR_ALLOC);

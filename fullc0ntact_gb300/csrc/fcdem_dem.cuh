@@ -1,9 +1,11 @@
 // fcdem_dem.cuh -- per-particle device arithmetic of the DEM step.
 //
-// Each function states the reference routine it reproduces.  The arithmetic
-// is written with the same operations in the same order as the reference, so
-// that the compiler forms the same fused multiply-adds and the results agree
-// bit for bit with the reference kernels built by the same nvcc.
+// Each function states the reference routine it reproduces, with the same
+// operations in the same order.  Where the reference's CUDA code leaves nvcc
+// to contract `a * b + c` into a fused multiply-add, the contraction is
+// written out here (fmaf, __fmul_rn, __fadd_rn): every kernel that inlines
+// these functions computes the same bits, and a CPU restatement with the
+// same fmaf calls reproduces them exactly.
 #pragma once
 
 #include "fcdem_internal.cuh"
@@ -56,26 +58,32 @@ __device__ __forceinline__ unsigned gridHash(int gx, int gy, int gz,
          __umul24(y, P.gridSize[0]) + x;
 }
 
+// The velocity and position update of particles_kernel.cu:55-59:
+// vel += gravity * dt (fused), vel *= globalDamping, pos += vel * dt (fused).
+__device__ __forceinline__ void advanceOne(float3 &p, float3 &v, float dt, const SimParams &P) {
+  v.x = fmaf(P.gravity[0], dt, v.x);
+  v.y = fmaf(P.gravity[1], dt, v.y);
+  v.z = fmaf(P.gravity[2], dt, v.z);
+  v.x = __fmul_rn(v.x, P.globalDamping);
+  v.y = __fmul_rn(v.y, P.globalDamping);
+  v.z = __fmul_rn(v.z, P.globalDamping);
+  p.x = fmaf(v.x, dt, p.x);
+  p.y = fmaf(v.y, dt, p.y);
+  p.z = fmaf(v.z, dt, p.z);
+}
+
 // particles_kernel.cu:39-75 (integrate_functor) on one particle; r is the
 // clamp radius (particleRadius, or pos.w in the polydisperse mode).
 __device__ __forceinline__ void integrateOne(float3 &p, float3 &v, float dt,
                                              float r, const SimParams &P) {
-  v.x = v.x + P.gravity[0] * dt;
-  v.y = v.y + P.gravity[1] * dt;
-  v.z = v.z + P.gravity[2] * dt;
-  v.x = v.x * P.globalDamping;
-  v.y = v.y * P.globalDamping;
-  v.z = v.z * P.globalDamping;
-  p.x = p.x + v.x * dt;
-  p.y = p.y + v.y * dt;
-  p.z = p.z + v.z * dt;
+  advanceOne(p, v, dt, P);
   const float bd = P.boundaryDamping;
-  if (p.x > 1.0f - r) { p.x = 1.0f - r; v.x = v.x * bd; }
-  if (p.x < -1.0f + r) { p.x = -1.0f + r; v.x = v.x * bd; }
-  if (p.y > 1.0f - r) { p.y = 1.0f - r; v.y = v.y * bd; }
-  if (p.z > 1.0f - r) { p.z = 1.0f - r; v.z = v.z * bd; }
-  if (p.z < -1.0f + r) { p.z = -1.0f + r; v.z = v.z * bd; }
-  if (p.y < -1.0f + r) { p.y = -1.0f + r; v.y = v.y * bd; }
+  if (p.x > 1.0f - r) { p.x = 1.0f - r; v.x = __fmul_rn(v.x, bd); }
+  if (p.x < -1.0f + r) { p.x = -1.0f + r; v.x = __fmul_rn(v.x, bd); }
+  if (p.y > 1.0f - r) { p.y = 1.0f - r; v.y = __fmul_rn(v.y, bd); }
+  if (p.z > 1.0f - r) { p.z = 1.0f - r; v.z = __fmul_rn(v.z, bd); }
+  if (p.z < -1.0f + r) { p.z = -1.0f + r; v.z = __fmul_rn(v.z, bd); }
+  if (p.y < -1.0f + r) { p.y = -1.0f + r; v.y = __fmul_rn(v.y, bd); }
 }
 
 // integrateOne with the box [lo, hi] instead of the reference's [-1, 1]^3
@@ -83,53 +91,51 @@ __device__ __forceinline__ void integrateOne(float3 &p, float3 &v, float dt,
 __device__ __forceinline__ void integrateOneBox(float3 &p, float3 &v, float dt, float r,
                                                 const SimParams &P, const float *lo,
                                                 const float *hi) {
-  v.x = v.x + P.gravity[0] * dt;
-  v.y = v.y + P.gravity[1] * dt;
-  v.z = v.z + P.gravity[2] * dt;
-  v.x = v.x * P.globalDamping;
-  v.y = v.y * P.globalDamping;
-  v.z = v.z * P.globalDamping;
-  p.x = p.x + v.x * dt;
-  p.y = p.y + v.y * dt;
-  p.z = p.z + v.z * dt;
+  advanceOne(p, v, dt, P);
   const float bd = P.boundaryDamping;
-  if (p.x > hi[0] - r) { p.x = hi[0] - r; v.x = v.x * bd; }
-  if (p.x < lo[0] + r) { p.x = lo[0] + r; v.x = v.x * bd; }
-  if (p.y > hi[1] - r) { p.y = hi[1] - r; v.y = v.y * bd; }
-  if (p.z > hi[2] - r) { p.z = hi[2] - r; v.z = v.z * bd; }
-  if (p.z < lo[2] + r) { p.z = lo[2] + r; v.z = v.z * bd; }
-  if (p.y < lo[1] + r) { p.y = lo[1] + r; v.y = v.y * bd; }
+  if (p.x > hi[0] - r) { p.x = hi[0] - r; v.x = __fmul_rn(v.x, bd); }
+  if (p.x < lo[0] + r) { p.x = lo[0] + r; v.x = __fmul_rn(v.x, bd); }
+  if (p.y > hi[1] - r) { p.y = hi[1] - r; v.y = __fmul_rn(v.y, bd); }
+  if (p.z > hi[2] - r) { p.z = hi[2] - r; v.z = __fmul_rn(v.z, bd); }
+  if (p.z < lo[2] + r) { p.z = lo[2] + r; v.z = __fmul_rn(v.z, bd); }
+  if (p.y < lo[1] + r) { p.y = lo[1] + r; v.y = __fmul_rn(v.y, bd); }
 }
 
 // The force of particles_kernel.cu:185-218 (collideSpheres) once the
 // distance test has passed: rel = pB - pA, dist = |rel|, cd = rA + rB.
+// norm = rel / dist (as rel * (1 / dist)); tanVel = relVel - dot(relVel,
+// norm) * norm; force = -spring (cd - dist) norm + damping relVel + shear
+// tanVel + attraction rel, each `+ a * b` fused.
 __device__ __forceinline__ float3 contactTerm(float3 rel, float dist, float cd,
                                               float3 vA, float3 vB,
                                               float attraction,
                                               const SimParams &P) {
-  float inv = 1.0f / dist;
-  float3 nrm = make_float3(rel.x * inv, rel.y * inv, rel.z * inv);
-  float3 rv = make_float3(vB.x - vA.x, vB.y - vA.y, vB.z - vA.z);
-  float dn = rv.x * nrm.x + rv.y * nrm.y + rv.z * nrm.z;
-  float3 tv = make_float3(rv.x - nrm.x * dn, rv.y - nrm.y * dn, rv.z - nrm.z * dn);
-  float s = -P.spring * (cd - dist);
-  float3 f = make_float3(nrm.x * s, nrm.y * s, nrm.z * s);
-  f.x = f.x + rv.x * P.damping;
-  f.y = f.y + rv.y * P.damping;
-  f.z = f.z + rv.z * P.damping;
-  f.x = f.x + tv.x * P.shear;
-  f.y = f.y + tv.y * P.shear;
-  f.z = f.z + tv.z * P.shear;
-  f.x = f.x + rel.x * attraction;
-  f.y = f.y + rel.y * attraction;
-  f.z = f.z + rel.z * attraction;
+  const float inv = __fdiv_rn(1.0f, dist);
+  const float3 nrm = make_float3(__fmul_rn(rel.x, inv), __fmul_rn(rel.y, inv),
+                                 __fmul_rn(rel.z, inv));
+  const float3 rv = make_float3(__fsub_rn(vB.x, vA.x), __fsub_rn(vB.y, vA.y),
+                                __fsub_rn(vB.z, vA.z));
+  const float dn = fmaf(rv.z, nrm.z, fmaf(rv.y, nrm.y, __fmul_rn(rv.x, nrm.x)));
+  const float3 tv = make_float3(fmaf(-nrm.x, dn, rv.x), fmaf(-nrm.y, dn, rv.y),
+                                fmaf(-nrm.z, dn, rv.z));
+  const float s = __fmul_rn(-P.spring, __fsub_rn(cd, dist));
+  float3 f = make_float3(__fmul_rn(nrm.x, s), __fmul_rn(nrm.y, s), __fmul_rn(nrm.z, s));
+  f.x = fmaf(rv.x, P.damping, f.x);
+  f.y = fmaf(rv.y, P.damping, f.y);
+  f.z = fmaf(rv.z, P.damping, f.z);
+  f.x = fmaf(tv.x, P.shear, f.x);
+  f.y = fmaf(tv.y, P.shear, f.y);
+  f.z = fmaf(tv.z, P.shear, f.z);
+  f.x = fmaf(rel.x, attraction, f.x);
+  f.y = fmaf(rel.y, attraction, f.y);
+  f.z = fmaf(rel.z, attraction, f.z);
   return f;
 }
 
-// |rel|^2 with the operations of length() (cutil_math.cuh: sqrtf(dot(v,v))),
-// so that sqrtf(pairDist2(rel)) is the reference's distance bit for bit.
+// |rel|^2 as length() (cutil_math.cuh: sqrtf(dot(v, v))) evaluates it, the
+// products fused into the sum: sqrtf(pairDist2(rel)) is the pair distance.
 __device__ __forceinline__ float pairDist2(float3 rel) {
-  return rel.x * rel.x + rel.y * rel.y + rel.z * rel.z;
+  return fmaf(rel.z, rel.z, fmaf(rel.y, rel.y, __fmul_rn(rel.x, rel.x)));
 }
 
 __device__ __forceinline__ float pairDist(float3 rel) { return sqrtf(pairDist2(rel)); }

@@ -95,15 +95,16 @@ void ParticleSystem::_initialize(int numParticles) {
   m_hVel = new float[n4]();
   m_hCellStart = new uint[m_numGridCells]();
   m_hCellEnd = new uint[m_numGridCells]();
-  size_t memSize = sizeof(float) * n4;
+  // byte counts as int, as particleSystem.cpp:117-190 passes them
+  const int memSize = (int)(sizeof(float) * n4);
   allocateArray((void **)&m_dPos, memSize);
   allocateArray((void **)&m_dVel, memSize);
   allocateArray((void **)&m_dSortedPos, memSize);
   allocateArray((void **)&m_dSortedVel, memSize);
-  allocateArray((void **)&m_dGridParticleHash, m_numParticles * sizeof(uint));
-  allocateArray((void **)&m_dGridParticleIndex, m_numParticles * sizeof(uint));
-  allocateArray((void **)&m_dCellStart, m_numGridCells * sizeof(uint));
-  allocateArray((void **)&m_dCellEnd, m_numGridCells * sizeof(uint));
+  allocateArray((void **)&m_dGridParticleHash, (int)(m_numParticles * sizeof(uint)));
+  allocateArray((void **)&m_dGridParticleIndex, (int)(m_numParticles * sizeof(uint)));
+  allocateArray((void **)&m_dCellStart, (int)(m_numGridCells * sizeof(uint)));
+  allocateArray((void **)&m_dCellEnd, (int)(m_numGridCells * sizeof(uint)));
   setParameters(&m_params);
   m_bInitialized = true;
 }

@@ -117,6 +117,16 @@ void radixSortPairs(Context &c, unsigned *keys, unsigned *vals, unsigned n,
 
 // Cell-table fill (cellStart = 0xffffffff).  Defined in fcdem_stages.cu.
 void fillU32(Context &c, unsigned *p, size_t count, unsigned value);
+// The stage kernels with an explicit parameter block, on the current stream
+// (fcdem_stages.cu): integrate (particles_kernel.cu:39-75), calcHash
+// (:97-115), and the reorder with cell-range detection (:119-182; the cell
+// tables must have been filled with 0xffffffff first).
+void launchIntegrate(float4 *pos, float4 *vel, float dt, unsigned n, const KParams &kp);
+void launchCalcHash(unsigned *hash, unsigned *index, const float4 *pos, unsigned n,
+                    const KParams &kp);
+void launchReorder(unsigned *cellStart, unsigned *cellEnd, float4 *sortedPos,
+                   float4 *sortedVel, const unsigned *hash, const unsigned *index,
+                   const float4 *oldPos, const float4 *oldVel, unsigned n, unsigned numCells);
 
 // The cell ranges collide reads: either the reference's cellStart/cellEnd
 // pair (empty = 0xffffffff start), or a prefix table off[] over numCells + 1

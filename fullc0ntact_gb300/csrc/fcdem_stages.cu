@@ -127,6 +127,19 @@ void launchIntegrateHash(float4 *pos, float4 *vel, float dt, unsigned *hash,
   launchOk();
 }
 
+void launchIntegrate(float4 *pos, float4 *vel, float dt, unsigned n, const KParams &kp) {
+  if (n == 0) return;
+  kIntegrate<<<(n + 255) / 256, 256, 0, curStream()>>>(pos, vel, dt, n, kp);
+  launchOk();
+}
+
+void launchCalcHash(unsigned *hash, unsigned *index, const float4 *pos, unsigned n,
+                    const KParams &kp) {
+  if (n == 0) return;
+  kCalcHash<<<(n + 255) / 256, 256, 0, curStream()>>>(hash, index, pos, n, kp);
+  launchOk();
+}
+
 void launchReorder(unsigned *cellStart, unsigned *cellEnd, float4 *sortedPos,
                    float4 *sortedVel, const unsigned *hash,
                    const unsigned *index, const float4 *oldPos,

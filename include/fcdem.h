@@ -67,9 +67,11 @@ struct cudaGraphicsResource;
 /* particleSystem.cu:39-63: selects a device.  "-device=N" in argv picks N,
  * otherwise device 0 (the GB300 build targets one GPU per process). */
 void cudaInit(int argc, char **argv);
-/* particleSystem.cu:65-68 (the implementation takes size_t; the reference
- * header says int). */
-void allocateArray(void **devPtr, size_t size);
+/* particleSystem.cu:65-68, with the argument type of the reference's header
+ * (particleSystem.cuh:16 declares int; its implementation takes size_t, a
+ * mismatch the reference's callers never see): size is a byte count below
+ * 2^31, a negative size records FCDEM_ERR_INVALID_VALUE. */
+void allocateArray(void **devPtr, int size);
 /* particleSystem.cu:70-73 */
 void freeArray(void *devPtr);
 /* particleSystem.cu:75-78: waits for all work issued by this library. */

@@ -18,6 +18,14 @@
 
 typedef struct { float x, y, z; } f3;
 
+/* Arithmetic mode (orc_set_gpu_arithmetic): 0 evaluates every a*b+c with
+ * two roundings, as the reference's code built for the host does; 1 fuses
+ * the products the reference's CUDA build contracts (nvcc's default), in
+ * the forms the GPU kernels of this repository spell out with fmaf. */
+static int g_gpu_arith = 0;
+
+void orc_set_gpu_arithmetic(int on) { g_gpu_arith = on ? 1 : 0; }
+
 static inline f3 mk3(float x, float y, float z) { f3 r = {x, y, z}; return r; }
 
 /* PTX cvt.rzi.s32.f32 semantics for the float->int conversion of the grid
@@ -61,17 +69,29 @@ void orc_integrate(const SimParams *P, float *pos, float *vel, float dt,
     float vx = v4[0], vy = v4[1], vz = v4[2];
     float r = radius_from_w ? p4[3] : P->particleRadius;
     float bd = P->boundaryDamping;
-    /* vel += gravity * deltaTime; vel *= globalDamping */
-    vx = vx + P->gravity[0] * dt;
-    vy = vy + P->gravity[1] * dt;
-    vz = vz + P->gravity[2] * dt;
+    /* vel += gravity * deltaTime; vel *= globalDamping; pos += vel * deltaTime
+     * (particles_kernel.cu:55-59) */
+    if (g_gpu_arith) {
+      vx = fmaf(P->gravity[0], dt, vx);
+      vy = fmaf(P->gravity[1], dt, vy);
+      vz = fmaf(P->gravity[2], dt, vz);
+    } else {
+      vx = vx + P->gravity[0] * dt;
+      vy = vy + P->gravity[1] * dt;
+      vz = vz + P->gravity[2] * dt;
+    }
     vx = vx * P->globalDamping;
     vy = vy * P->globalDamping;
     vz = vz * P->globalDamping;
-    /* pos += vel * deltaTime */
-    px = px + vx * dt;
-    py = py + vy * dt;
-    pz = pz + vz * dt;
+    if (g_gpu_arith) {
+      px = fmaf(vx, dt, px);
+      py = fmaf(vy, dt, py);
+      pz = fmaf(vz, dt, pz);
+    } else {
+      px = px + vx * dt;
+      py = py + vy * dt;
+      pz = pz + vz * dt;
+    }
     /* faces in the reference's order: +x, -x, +y, +z, -z, -y */
     if (px > 1.0f - r) { px = 1.0f - r; vx = vx * bd; }
     if (px < -1.0f + r) { px = -1.0f + r; vx = vx * bd; }
@@ -147,9 +167,40 @@ void orc_reorder(unsigned *cellStart, unsigned *cellEnd, float *sortedPos,
 }
 
 /* ---------------------------------------------------------------------- */
+/* particles_kernel.cu:185-218 with the products nvcc contracts fused: the
+ * distance as sqrtf(dot(rel, rel)), each `x + a * b` of the normal
+ * projection and the force sum as one fmaf. */
+static inline f3 sphere_term_fused(f3 pA, f3 pB, f3 vA, f3 vB, float rA, float rB,
+                                   float attraction, const SimParams *P) {
+  f3 rel = mk3(pB.x - pA.x, pB.y - pA.y, pB.z - pA.z);
+  float dist = sqrtf(fmaf(rel.z, rel.z, fmaf(rel.y, rel.y, rel.x * rel.x)));
+  float cd = rA + rB;
+  f3 f = mk3(0.0f, 0.0f, 0.0f);
+  if (dist < cd) {
+    float inv = 1.0f / dist;
+    f3 nrm = mk3(rel.x * inv, rel.y * inv, rel.z * inv);
+    f3 rv = mk3(vB.x - vA.x, vB.y - vA.y, vB.z - vA.z);
+    float dn = fmaf(rv.z, nrm.z, fmaf(rv.y, nrm.y, rv.x * nrm.x));
+    f3 tv = mk3(fmaf(-nrm.x, dn, rv.x), fmaf(-nrm.y, dn, rv.y), fmaf(-nrm.z, dn, rv.z));
+    float s = -P->spring * (cd - dist);
+    f.x = nrm.x * s; f.y = nrm.y * s; f.z = nrm.z * s;
+    f.x = fmaf(rv.x, P->damping, f.x);
+    f.y = fmaf(rv.y, P->damping, f.y);
+    f.z = fmaf(rv.z, P->damping, f.z);
+    f.x = fmaf(tv.x, P->shear, f.x);
+    f.y = fmaf(tv.y, P->shear, f.y);
+    f.z = fmaf(tv.z, P->shear, f.z);
+    f.x = fmaf(rel.x, attraction, f.x);
+    f.y = fmaf(rel.y, attraction, f.y);
+    f.z = fmaf(rel.z, attraction, f.z);
+  }
+  return f;
+}
+
 /* particles_kernel.cu:185-218, float.  Returns the pair term. */
 static inline f3 sphere_term(f3 pA, f3 pB, f3 vA, f3 vB, float rA, float rB,
                              float attraction, const SimParams *P) {
+  if (g_gpu_arith) return sphere_term_fused(pA, pB, vA, vB, rA, rB, attraction, P);
   f3 rel = mk3(pB.x - pA.x, pB.y - pA.y, pB.z - pA.z);
   float dist = sqrtf(rel.x * rel.x + rel.y * rel.y + rel.z * rel.z);
   float cd = rA + rB;
@@ -380,6 +431,9 @@ void orc_update(const SimParams *P, float dt, float *pos, float *vel,
 /* ---------------------------------------------------------------------- */
 /* Distance map. */
 
+static int check_distmap_fused(const orc_distmap *m, float r, float bd, float p[3],
+                               float v[3]);
+
 static inline int clampi(int v, int lo, int hi) {
   return v < lo ? lo : (v > hi ? hi : v);
 }
@@ -477,22 +531,37 @@ void orc_integrate_distmap(const SimParams *P, const orc_distmap *m,
     float p[3] = {p4[0], p4[1], p4[2]}, v[3] = {v4[0], v4[1], v4[2]};
     float r = radius_from_w ? p4[3] : P->particleRadius;
     float bd = P->boundaryDamping;
-    for (int k = 0; k < 3; ++k) v[k] = v[k] + P->gravity[k] * dt;
-    for (int k = 0; k < 3; ++k) v[k] = v[k] * P->globalDamping;
-    for (int k = 0; k < 3; ++k) p[k] = p[k] + v[k] * dt;
+    if (g_gpu_arith) {
+      for (int k = 0; k < 3; ++k) v[k] = fmaf(P->gravity[k], dt, v[k]);
+      for (int k = 0; k < 3; ++k) v[k] = v[k] * P->globalDamping;
+      for (int k = 0; k < 3; ++k) p[k] = fmaf(v[k], dt, p[k]);
+    } else {
+      for (int k = 0; k < 3; ++k) v[k] = v[k] + P->gravity[k] * dt;
+      for (int k = 0; k < 3; ++k) v[k] = v[k] * P->globalDamping;
+      for (int k = 0; k < 3; ++k) p[k] = p[k] + v[k] * dt;
+    }
     /* d_checkBoundaryDistMap, boundaries.cuh:65-89: the cylinder test uses
      * the position before the map push. */
-    float len = sqrtf(p[0] * p[0] + p[1] * p[1] + 0.0f * 0.0f);
+    float l2 = g_gpu_arith ? fmaf(p[0], p[0], p[1] * p[1])
+                           : p[0] * p[0] + p[1] * p[1] + 0.0f * 0.0f;
+    float len = sqrtf(l2);
     float px0 = p[0], py0 = p[1];
-    orc_check_distmap(m, r, bd, p, v);
+    if (g_gpu_arith) check_distmap_fused(m, r, bd, p, v);
+    else orc_check_distmap(m, r, bd, p, v);
     if (len > 1.0f) {
       float pen = len - 1.0f;
-      float invLen = 1.0f / sqrtf(px0 * px0 + py0 * py0 + 0.0f * 0.0f);
+      float invLen = 1.0f / sqrtf(l2);
       float nx = px0 * invLen, ny = py0 * invLen, nz = 0.0f * invLen;
       float s = pen + r;
-      p[0] = p[0] - nx * s;
-      p[1] = p[1] - ny * s;
-      p[2] = p[2] - nz * s;
+      if (g_gpu_arith) {
+        p[0] = fmaf(-nx, s, p[0]);
+        p[1] = fmaf(-ny, s, p[1]);
+        p[2] = fmaf(-nz, s, p[2]);
+      } else {
+        p[0] = p[0] - nx * s;
+        p[1] = p[1] - ny * s;
+        p[2] = p[2] - nz * s;
+      }
       v[0] = v[0] * bd;
       v[1] = v[1] * bd;
     }
@@ -584,6 +653,29 @@ static void distmap_query_fused(const orc_distmap *m, const float q[3],
   }
 }
 
+/* checkDistMap (boundaries.cuh:38-63) as the GPU build evaluates it: the
+ * fused contact-point blend, the normal's squared length and the two
+ * position updates as fmaf; rsqrtf restated as 1/sqrtf (the GPU's rsqrtf is
+ * within 2 ulp of it).  Returns 1 when the map pushed the particle. */
+static int check_distmap_fused(const orc_distmap *m, float r, float bd, float p[3],
+                               float v[3]) {
+  float dist = 0.0f, cp[3] = {0.0f, 0.0f, 0.0f};
+  distmap_query_fused(m, p, &dist, cp);
+  if (!(dist < r)) return 0;
+  float n0[3] = {p[0] - cp[0], p[1] - cp[1], p[2] - cp[2]};
+  float dd = fmaf(n0[0], n0[0], fmaf(n0[1], n0[1], n0[2] * n0[2]));
+  float invLen = 1.0f / sqrtf(dd);
+  float nn[3] = {n0[0] * invLen, n0[1] * invLen, n0[2] * invLen};
+  float pen = r - dist;
+  float extra = (float)(0.1 * (double)r);
+  for (int k = 0; k < 3; ++k) p[k] = fmaf(nn[k], pen, p[k]);
+  for (int k = 0; k < 3; ++k) p[k] = fmaf(nn[k], extra, p[k]);
+  v[0] = v[0] * (0.5f * bd);
+  v[1] = v[1] * (0.5f * bd);
+  v[2] = v[2] * (0.7f * bd);
+  return 1;
+}
+
 void orc_batch_obstacle_integrate(const SimParams *P, const float lo[3],
                                   const float hi[3], const orc_distmap *m,
                                   float *pos, float *vel, float dt, unsigned n,
@@ -599,27 +691,7 @@ void orc_batch_obstacle_integrate(const SimParams *P, const float lo[3],
     for (int k = 0; k < 3; ++k) v[k] = fmaf(P->gravity[k], dt, v[k]);
     for (int k = 0; k < 3; ++k) v[k] = v[k] * P->globalDamping;
     for (int k = 0; k < 3; ++k) p[k] = fmaf(v[k], dt, p[k]);
-    if (m) {
-      /* checkDistMap, boundaries.cuh:38-63 */
-      float dist = 0.0f, cp[3] = {0.0f, 0.0f, 0.0f};
-      distmap_query_fused(m, p, &dist, cp);
-      if (dist < r) {
-        float n0[3] = {p[0] - cp[0], p[1] - cp[1], p[2] - cp[2]};
-        /* normalize = v * rsqrtf(dot(v, v)); rsqrtf restated as 1/sqrtf
-         * (the GPU's rsqrtf is within 2 ulp of it) */
-        float dd = fmaf(n0[0], n0[0], fmaf(n0[1], n0[1], n0[2] * n0[2]));
-        float invLen = 1.0f / sqrtf(dd);
-        float nn[3] = {n0[0] * invLen, n0[1] * invLen, n0[2] * invLen};
-        float pen = r - dist;
-        float extra = (float)(0.1 * (double)r);
-        for (int k = 0; k < 3; ++k) p[k] = fmaf(nn[k], pen, p[k]);
-        for (int k = 0; k < 3; ++k) p[k] = fmaf(nn[k], extra, p[k]);
-        v[0] = v[0] * (0.5f * bd);
-        v[1] = v[1] * (0.5f * bd);
-        v[2] = v[2] * (0.7f * bd);
-        ++nc;
-      }
-    }
+    if (m) nc += (unsigned)check_distmap_fused(m, r, bd, p, v); /* boundaries.cuh:38-63 */
     box_faces(l, h, r, bd, p, v);
     p4[0] = p[0]; p4[1] = p[1]; p4[2] = p[2];
     v4[0] = v[0]; v4[1] = v[1]; v4[2] = v[2];

@@ -19,6 +19,14 @@
 extern "C" {
 #endif
 
+/* Arithmetic of the restatement.  0 (default): every a*b+c with two
+ * roundings, as the reference's code compiled for the host (the golden
+ * fixtures) computes it.  1: the products that nvcc contracts in the
+ * reference's CUDA build fused (fmaf), in the forms the GPU kernels of this
+ * repository spell out -- integrate, the pair distance and the pair force.
+ * Process-wide; the tests set it around a comparison. */
+void orc_set_gpu_arithmetic(int on);
+
 /* particles_kernel.cu:39-75 (integrate_functor).  radius_from_w selects the
  * polydisperse extension (clamp with pos.w instead of particleRadius). */
 void orc_integrate(const SimParams *P, float *pos, float *vel, float dt,

@@ -105,6 +105,8 @@ def lib():
         L.orc_distmap_query.argtypes = [C.POINTER(DistMap), _f32p, C.POINTER(C.c_float), _f32p]
         L.orc_integrate_distmap.argtypes = [P, C.POINTER(DistMap), _f32p, _f32p,
                                             C.c_float, C.c_uint, C.c_int]
+        L.orc_set_gpu_arithmetic.argtypes = [C.c_int]
+        L.orc_set_gpu_arithmetic.restype = None
         L.orc_integrate_box.argtypes = [P, _f32p, _f32p, _f32p, _f32p, C.c_float, C.c_uint,
                                         C.c_int]
         L.orc_batch_obstacle_integrate.argtypes = [P, _f32p, _f32p, C.c_void_p, _f32p, _f32p,
@@ -212,6 +214,20 @@ def ref_distmap():
         L.fcref_um_integrate.restype = None
         L._typed = True
     return L
+
+
+class gpu_arithmetic:
+    """Context manager: the oracle evaluates with the products nvcc contracts
+    fused (orc_set_gpu_arithmetic), the arithmetic the GPU kernels spell out;
+    on exit back to the host arithmetic of the reference's host build."""
+
+    def __enter__(self):
+        lib().orc_set_gpu_arithmetic(1)
+        return self
+
+    def __exit__(self, *exc):
+        lib().orc_set_gpu_arithmetic(0)
+        return False
 
 
 def lattice_coords(vmin, cell_size, cells):
