@@ -780,6 +780,234 @@ kCollideTiled(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
                                                 out, P);
 }
 
+// ---------------------------------------------------------------------------
+// Warp-cooperative collide over the prefix cell table (linear cell order).
+//
+// The lanes of a warp hold 32 consecutive sorted particles.  For each of the
+// nine neighbour rows every particle has one range of candidate partners
+// (the row's three cells are consecutive hashes when x does not wrap).  The
+// (particle, partner) pairs of the warp's 32 ranges are cut into 32 chunks
+// of equal length, one per lane, so that every lane tests as many
+// candidates as any other, whatever the spread of the ranges; a lane walks
+// its chunk in (particle, partner) order and moves to the next particle's
+// range when it reaches its end.  A candidate below the squared-distance
+// bound (rejectBound) goes to its particle's list of near partners in
+// shared memory, keyed by (neighbour cell, sorted index).  After the nine
+// rows each lane sorts its own particle's list -- which is then in the
+// reference's order: cells in z, y, x order, partners in ascending sorted
+// index -- and runs the exact test and the contact terms in that order,
+// with the cell subtotals of collideCell (particles_kernel.cu:223-285).  The
+// sums are kCollideGlobal's bit for bit.
+//
+// A particle whose row would wrap in x, or whose list overflows, is handed
+// to kCollideCrowd as a group of one (that kernel walks any particle's 27
+// cells in the reference's order); a particle in a crowded neighbourhood is
+// deferred there as in kCollideGlobal.
+constexpr int kWarpWarps = 4;            // warps per CTA
+constexpr int kListCap = 32;             // near partners per particle
+constexpr int kWarpStage = 160;          // staged partner positions per warp and row
+constexpr unsigned kKeyCellShift = 27;   // list key: neighbour cell << 27 | sorted index
+constexpr unsigned kKeyIndexMask = (1u << kKeyCellShift) - 1u;
+
+struct __align__(16) WarpSmem {
+  float4 stage[kWarpStage];      // the row's partners, when their union is short
+  float4 me[32];                 // each lane's particle: x, y, z, radius
+  unsigned list[kListCap][32];   // [entry][lane]: one bank per lane
+  unsigned count[32];
+  unsigned pre[33];              // exclusive prefix of the row's range lengths
+  unsigned a[32], o1[32], o2[32];  // range start; its cell boundaries
+};
+
+__device__ __forceinline__ void deferOne(const CrowdList &crowd, unsigned i) {
+  const unsigned k = atomicAdd(crowd.count, 1u);
+  if (k < crowd.cap) crowd.groups[k] = make_uint2(i, 1u);
+}
+
+template <int kMode, bool kRadiusFromW, bool kCollider, bool kForceOut>
+__global__ void __launch_bounds__(kWarpWarps * 32)
+kCollideWarp(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
+             const float4 *__restrict__ sortedVel, const unsigned *__restrict__ index,
+             CellRanges cells, unsigned n, KParams kp, CollideOut out, bool cull,
+             CrowdList crowd, unsigned *status) {
+  __shared__ WarpSmem smAll[kWarpWarps];
+  const SimParams &P = kp.p;
+  const unsigned lane = threadIdx.x & 31u;
+  WarpSmem &sm = smAll[threadIdx.x >> 5];
+  const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = i < n;
+  float4 p4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), v4 = p4;
+  if (valid) {
+    p4 = ldg4(sortedPos + i);
+    v4 = ldg4(sortedVel + i);
+  }
+  const float3 pos = make_float3(p4.x, p4.y, p4.z), vel = make_float3(v4.x, v4.y, v4.z);
+  const float ri = kRadiusFromW ? p4.w : P.particleRadius;
+  const int3 g = gridPos(pos.x, pos.y, pos.z, P);
+  bool mine = valid;  // this kernel finishes the particle
+  if (mine && neighbourhoodCount<true>(g, cells, n, P) > crowd.limit) {
+    unsigned a, b;
+    cellRange<true>(gridHash(g.x, g.y, g.z, P), cells, n, a, b);
+    if (i >= a && i < b) {  // deferred to kCollideCrowd with its cell's members
+      if (((i - a) & 31u) == 0u) {
+        const unsigned k = atomicAdd(crowd.count, 1u);
+        if (k < crowd.cap) crowd.groups[k] = make_uint2(i, min(32u, b - i));
+      }
+      mine = false;
+    }
+  }
+  bool lcull = cull;
+  if (mine && kRadiusFromW && !(ri <= P.particleRadius)) {
+    atomicOr(status, (unsigned)kStatusRadiusBound);
+    lcull = false;
+  }
+  const unsigned gxm = P.gridSize[0] - 1u;
+  const unsigned xm = (unsigned)g.x & gxm;
+  if (mine && !inertPos(pos) && !(xm >= 1u && xm < gxm)) {  // the row wraps in x
+    deferOne(crowd, i);
+    mine = false;
+  }
+  // an inert particle's force is +0.0 (inertPos): it scans nothing
+  const bool scan = mine && !inertPos(pos);
+  const float cdMono = ri + P.particleRadius;
+  const float cdMonoHi2 = rejectBound(cdMono);
+  const CellCull cc = makeCull(pos, g, ri + P.particleRadius, P);
+  const float cullR2 = lcull ? cc.r2 : __int_as_float(0x7f800000);
+  sm.me[lane] = make_float4(pos.x, pos.y, pos.z, ri);
+  sm.count[lane] = 0u;
+  __syncwarp();
+#pragma unroll 1
+  for (int row = 0; row < 9; row++) {
+    const int z = row / 3 - 1, y = row % 3 - 1;
+    unsigned a = 0u, b = 0u, o1 = 0u, o2 = 0u;
+    if (scan) {
+      const float rowD2 = CellCull::pick(z, cc.zl, cc.zh) + CellCull::pick(y, cc.yl, cc.yh);
+      if (rowD2 <= cullR2) {
+        const bool useL = rowD2 + cc.xl <= cullR2;
+        const bool useR = rowD2 + cc.xh <= cullR2;
+        const unsigned h0 = gridHash(g.x - 1, g.y + y, g.z + z, P);
+        const unsigned q0 = __ldg(cells.off + h0);
+        o1 = __ldg(cells.off + h0 + 1);
+        o2 = __ldg(cells.off + h0 + 2);
+        const unsigned q3 = __ldg(cells.off + h0 + 3);
+        a = useL ? q0 : o1;
+        b = min(useR ? q3 : o2, n);
+        if (b < a) b = a;
+      }
+    }
+    const unsigned len = b - a;
+    unsigned incl = len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+      if ((int)lane >= o) incl += t;
+    }
+    const unsigned total = __shfl_sync(0xffffffffu, incl, 31);
+    if (total == 0u) continue;  // warp-uniform
+    sm.pre[lane + 1] = incl;
+    if (lane == 0) sm.pre[0] = 0u;
+    sm.a[lane] = a;
+    sm.o1[lane] = o1;
+    sm.o2[lane] = o2;
+    // The lanes' ranges mostly overlap (consecutive particles, mostly one
+    // grid row): their union is copied to shared memory with coalesced
+    // loads when it is short.
+    const unsigned lo = __reduce_min_sync(0xffffffffu, len ? a : 0xffffffffu);
+    const unsigned hi = __reduce_max_sync(0xffffffffu, len ? b : 0u);
+    const bool staged = hi - lo <= (unsigned)kWarpStage;
+    if (staged)
+      for (unsigned t = lane; t < hi - lo; t += 32u) sm.stage[t] = ldg4(sortedPos + lo + t);
+    __syncwarp();
+    const unsigned chunk = (total + 31u) >> 5;
+    unsigned k = lane * chunk;
+    const unsigned kEnd = min(k + chunk, total);
+    if (k < kEnd) {
+      // the particle whose range holds pair k: the last il with pre[il] <= k
+      // (pre[32] = total > k, so il <= 31 and pre[il + 1] > k)
+      unsigned il = 0u;
+#pragma unroll
+      for (unsigned st = 16u; st; st >>= 1)
+        if (sm.pre[il + st] <= k) il += st;
+      float4 me = sm.me[il];
+      unsigned next = sm.pre[il + 1];
+      unsigned j = sm.a[il] + (k - sm.pre[il]);
+      unsigned m1 = sm.o1[il], m2 = sm.o2[il];
+      for (; k < kEnd; ++k, ++j) {
+        if (k == next) {  // the next particle with a non-empty range
+          do {
+            ++il;
+            next = sm.pre[il + 1];
+          } while (next == k);
+          me = sm.me[il];
+          j = sm.a[il];
+          m1 = sm.o1[il];
+          m2 = sm.o2[il];
+        }
+        const float4 q4 = staged ? sm.stage[j - lo] : ldg4(sortedPos + j);
+        const float3 rel = make_float3(q4.x - me.x, q4.y - me.y, q4.z - me.z);
+        const float d2 = pairDist2(rel);
+        const float hi2 = kRadiusFromW ? rejectBound(me.w + q4.w) : cdMonoHi2;
+        if (d2 < hi2) {  // the particle itself too (d2 = 0): skipped in the drain
+          const unsigned cell = (unsigned)row * 3u + (j >= m1) + (j >= m2);
+          const unsigned slot = atomicAdd(&sm.count[il], 1u);
+          if (slot < (unsigned)kListCap) sm.list[slot][il] = (cell << kKeyCellShift) | j;
+        }
+      }
+    }
+    __syncwarp();  // the staged rows and range arrays are reused by the next row
+  }
+  if (!mine) return;
+  float3 force = make_float3(0.0f, 0.0f, 0.0f);
+  if (scan) {
+    const unsigned c = sm.count[lane];
+    if (c > (unsigned)kListCap) {  // more near partners than the list holds
+      deferOne(crowd, i);
+      return;
+    }
+    // insertion sort: (cell, sorted index) ascending is the reference's order
+    for (unsigned t = 1; t < c; ++t) {
+      const unsigned key = sm.list[t][lane];
+      unsigned s = t;
+      while (s > 0u && sm.list[s - 1][lane] > key) {
+        sm.list[s][lane] = sm.list[s - 1][lane];
+        --s;
+      }
+      sm.list[s][lane] = key;
+    }
+    float3 cf = make_float3(0.0f, 0.0f, 0.0f);
+    int cfCell = -1;
+    for (unsigned t = 0; t < c; ++t) {
+      const unsigned key = sm.list[t][lane];
+      const unsigned j = key & kKeyIndexMask;
+      if (j == i) continue;
+      const int cell = (int)(key >> kKeyCellShift);
+      const float4 q4 = ldg4(sortedPos + j);
+      const float3 rel = make_float3(q4.x - pos.x, q4.y - pos.y, q4.z - pos.z);
+      const float dist = sqrtf(pairDist2(rel));
+      const float cd = kRadiusFromW ? ri + q4.w : cdMono;
+      if (dist < cd) {
+        if (cell != cfCell) {
+          force.x = force.x + cf.x;
+          force.y = force.y + cf.y;
+          force.z = force.z + cf.z;
+          cf = make_float3(0.0f, 0.0f, 0.0f);
+          cfCell = cell;
+        }
+        const float4 w4 = ldg4(sortedVel + j);
+        const float3 f = contactTerm(rel, dist, cd, vel, make_float3(w4.x, w4.y, w4.z),
+                                     P.attraction, P);
+        cf.x = cf.x + f.x;
+        cf.y = cf.y + f.y;
+        cf.z = cf.z + f.z;
+      }
+    }
+    force.x = force.x + cf.x;
+    force.y = force.y + cf.y;
+    force.z = force.z + cf.z;
+  }
+  finishParticle<kMode, kCollider, kForceOut>(i, n, pos, vel, p4, ri, force, index, newVel, out,
+                                              P);
+}
+
 bool g_crowdPath = true;  // fcdemSetCrowdPath
 unsigned g_crowdLimit = kCrowdLimit;  // fcdemSetCrowdLimit
 constexpr unsigned kCrowdCtasPerSm = 4;  // persistent grid: this many CTAs per SM
@@ -811,7 +1039,7 @@ CrowdList crowdList(unsigned n) {
 }
 
 template <int kMode, bool kRadiusFromW, bool kCollider, bool kForceOut, bool kPrefix>
-void launchT(bool tiled, bool cull, unsigned n, float4 *newVel, const float4 *sp,
+void launchT(bool tiled, bool warpPath, bool cull, unsigned n, float4 *newVel, const float4 *sp,
              const float4 *sv, const unsigned *index, const CellRanges &cells,
              const KParams &kp, const CollideOut &out) {
   unsigned blocks = (n + 127) / 128;
@@ -819,7 +1047,24 @@ void launchT(bool tiled, bool cull, unsigned n, float4 *newVel, const float4 *sp
     kCollideTiled<kMode, kRadiusFromW, kCollider, kForceOut>
         <<<blocks, kTileThreads, 0, curStream()>>>(newVel, sp, sv, index, cells, n, kp, out,
                                                    ctx().dStatus);
-  else {
+  else if (kPrefix && warpPath && kp.p.maxParticlesPerCell != kMortonTag &&
+           n <= kKeyIndexMask) {
+    // the warp-cooperative kernel; its deferred particles (crowded, x-wrapping,
+    // list overflow) go to kCollideCrowd
+    CrowdList crowd = crowdList(n);
+    if (crowd.groups) {
+      kCollideWarp<kMode, kRadiusFromW, kCollider, kForceOut>
+          <<<(n + kWarpWarps * 32 - 1) / (kWarpWarps * 32), kWarpWarps * 32, 0, curStream()>>>(
+              newVel, sp, sv, index, cells, n, kp, out, cull, crowd, ctx().dStatus);
+      if (launchOk())
+        kCollideCrowd<kMode, kRadiusFromW, kCollider, kForceOut, kPrefix>
+            <<<numSms() * kCrowdCtasPerSm, kCrowdWarps * 32, 0, curStream()>>>(
+                newVel, sp, sv, index, cells, n, kp, out, cull, crowd, ctx().dStatus);
+      return;
+    }
+    warpPath = false;  // no group list: the per-thread kernel covers every particle
+  }
+  if (!(tiled && !kPrefix)) {
     const CrowdList crowd = crowdList(n);
     kCollideGlobal<kMode, kRadiusFromW, kCollider, kForceOut, kPrefix>
         <<<blocks, 128, 0, curStream()>>>(newVel, sp, sv, index, cells, n, kp, out, cull,
@@ -899,7 +1144,7 @@ kCollideBatch(const BatchScene *__restrict__ scenes, const unsigned *__restrict_
   }
 }
 
-int g_collidePath = -1;  // -1 auto, 0 global, 1 tiled (fcdemSetCollidePath)
+int g_collidePath = -1;  // -1 auto, 0 global, 1 tiled, 2 warp (fcdemSetCollidePath)
 bool g_cullCells = true;  // fcdemSetCellCulling
 
 }  // namespace
@@ -914,6 +1159,8 @@ void launchCollide(int mode, bool collider, float4 *newVel, const float4 *sp,
   // (its row windows assume the linear cell order)
   bool tiled = !prefix && g_collidePath == 1 && ((uintptr_t)sp & 15u) == 0 &&
                kp.p.maxParticlesPerCell != kMortonTag;
+  // the warp-cooperative kernel needs the prefix table and the group list
+  const bool warpPath = prefix && g_crowdPath && g_collidePath == 2;
   // Culling is exact when every grid dimension is >= 3 and the largest
   // contact distance 2 * particleRadius fits in the smallest cell.
   const SimParams &P = kp.p;
@@ -925,7 +1172,7 @@ void launchCollide(int mode, bool collider, float4 *newVel, const float4 *sp,
   const bool fo = out.force != nullptr;
 #define FCDEM_COLLIDE_CASE(M, W, C, F, X)                                              \
   if (mode == M && w == W && collider == C && fo == F && prefix == X) {                \
-    launchT<M, W, C, F, X>(tiled, cull, n, newVel, sp, sv, index, cells, kp, out);     \
+    launchT<M, W, C, F, X>(tiled, warpPath, cull, n, newVel, sp, sv, index, cells, kp, out); \
     launchOk();                                                                        \
     return;                                                                            \
   }
@@ -986,7 +1233,7 @@ void launchCollideBatch(int mode, bool radiusFromW, const BatchScene *scenes,
 }  // namespace fcdem
 
 extern "C" void fcdemSetCollidePath(int path) {
-  fcdem::g_collidePath = (path == 0 || path == 1) ? path : -1;
+  fcdem::g_collidePath = (path >= 0 && path <= 2) ? path : -1;
 }
 
 extern "C" void fcdemSetCellCulling(int on) { fcdem::g_cullCells = on != 0; }

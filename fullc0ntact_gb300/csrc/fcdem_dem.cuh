@@ -105,7 +105,9 @@ __device__ __forceinline__ void integrateOneBox(float3 &p, float3 &v, float dt, 
 // distance test has passed: rel = pB - pA, dist = |rel|, cd = rA + rB.
 // norm = rel / dist (as rel * (1 / dist)); tanVel = relVel - dot(relVel,
 // norm) * norm; force = -spring (cd - dist) norm + damping relVel + shear
-// tanVel + attraction rel, each `+ a * b` fused.
+// tanVel + attraction rel.  The fusions are the ones nvcc forms from the
+// reference's expressions: in `a * b + c * d` the left product is fused
+// with the right one as addend; in `x + a * b` the product is fused.
 __device__ __forceinline__ float3 contactTerm(float3 rel, float dist, float cd,
                                               float3 vA, float3 vB,
                                               float attraction,
@@ -115,14 +117,13 @@ __device__ __forceinline__ float3 contactTerm(float3 rel, float dist, float cd,
                                  __fmul_rn(rel.z, inv));
   const float3 rv = make_float3(__fsub_rn(vB.x, vA.x), __fsub_rn(vB.y, vA.y),
                                 __fsub_rn(vB.z, vA.z));
-  const float dn = fmaf(rv.z, nrm.z, fmaf(rv.y, nrm.y, __fmul_rn(rv.x, nrm.x)));
+  const float dn = fmaf(rv.z, nrm.z, fmaf(rv.x, nrm.x, __fmul_rn(rv.y, nrm.y)));
   const float3 tv = make_float3(fmaf(-nrm.x, dn, rv.x), fmaf(-nrm.y, dn, rv.y),
                                 fmaf(-nrm.z, dn, rv.z));
   const float s = __fmul_rn(-P.spring, __fsub_rn(cd, dist));
-  float3 f = make_float3(__fmul_rn(nrm.x, s), __fmul_rn(nrm.y, s), __fmul_rn(nrm.z, s));
-  f.x = fmaf(rv.x, P.damping, f.x);
-  f.y = fmaf(rv.y, P.damping, f.y);
-  f.z = fmaf(rv.z, P.damping, f.z);
+  float3 f = make_float3(fmaf(s, nrm.x, __fmul_rn(P.damping, rv.x)),
+                         fmaf(s, nrm.y, __fmul_rn(P.damping, rv.y)),
+                         fmaf(s, nrm.z, __fmul_rn(P.damping, rv.z)));
   f.x = fmaf(tv.x, P.shear, f.x);
   f.y = fmaf(tv.y, P.shear, f.y);
   f.z = fmaf(tv.z, P.shear, f.z);
@@ -133,9 +134,10 @@ __device__ __forceinline__ float3 contactTerm(float3 rel, float dist, float cd,
 }
 
 // |rel|^2 as length() (cutil_math.cuh: sqrtf(dot(v, v))) evaluates it, the
-// products fused into the sum: sqrtf(pairDist2(rel)) is the pair distance.
+// products fused into the sum as in contactTerm: sqrtf(pairDist2(rel)) is
+// the pair distance.
 __device__ __forceinline__ float pairDist2(float3 rel) {
-  return fmaf(rel.z, rel.z, fmaf(rel.y, rel.y, __fmul_rn(rel.x, rel.x)));
+  return fmaf(rel.z, rel.z, fmaf(rel.x, rel.x, __fmul_rn(rel.y, rel.y)));
 }
 
 __device__ __forceinline__ float pairDist(float3 rel) { return sqrtf(pairDist2(rel)); }

@@ -167,26 +167,26 @@ void orc_reorder(unsigned *cellStart, unsigned *cellEnd, float *sortedPos,
 }
 
 /* ---------------------------------------------------------------------- */
-/* particles_kernel.cu:185-218 with the products nvcc contracts fused: the
- * distance as sqrtf(dot(rel, rel)), each `x + a * b` of the normal
- * projection and the force sum as one fmaf. */
+/* particles_kernel.cu:185-218 with the products nvcc contracts fused: in
+ * `a * b + c * d` the left product is fused with the right one as addend,
+ * in `x + a * b` the product is fused (dot products, the tangential
+ * velocity, the force sum). */
 static inline f3 sphere_term_fused(f3 pA, f3 pB, f3 vA, f3 vB, float rA, float rB,
                                    float attraction, const SimParams *P) {
   f3 rel = mk3(pB.x - pA.x, pB.y - pA.y, pB.z - pA.z);
-  float dist = sqrtf(fmaf(rel.z, rel.z, fmaf(rel.y, rel.y, rel.x * rel.x)));
+  float dist = sqrtf(fmaf(rel.z, rel.z, fmaf(rel.x, rel.x, rel.y * rel.y)));
   float cd = rA + rB;
   f3 f = mk3(0.0f, 0.0f, 0.0f);
   if (dist < cd) {
     float inv = 1.0f / dist;
     f3 nrm = mk3(rel.x * inv, rel.y * inv, rel.z * inv);
     f3 rv = mk3(vB.x - vA.x, vB.y - vA.y, vB.z - vA.z);
-    float dn = fmaf(rv.z, nrm.z, fmaf(rv.y, nrm.y, rv.x * nrm.x));
+    float dn = fmaf(rv.z, nrm.z, fmaf(rv.x, nrm.x, rv.y * nrm.y));
     f3 tv = mk3(fmaf(-nrm.x, dn, rv.x), fmaf(-nrm.y, dn, rv.y), fmaf(-nrm.z, dn, rv.z));
     float s = -P->spring * (cd - dist);
-    f.x = nrm.x * s; f.y = nrm.y * s; f.z = nrm.z * s;
-    f.x = fmaf(rv.x, P->damping, f.x);
-    f.y = fmaf(rv.y, P->damping, f.y);
-    f.z = fmaf(rv.z, P->damping, f.z);
+    f.x = fmaf(s, nrm.x, P->damping * rv.x);
+    f.y = fmaf(s, nrm.y, P->damping * rv.y);
+    f.z = fmaf(s, nrm.z, P->damping * rv.z);
     f.x = fmaf(tv.x, P->shear, f.x);
     f.y = fmaf(tv.y, P->shear, f.y);
     f.z = fmaf(tv.z, P->shear, f.z);

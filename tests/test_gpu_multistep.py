@@ -10,9 +10,12 @@ in a 256^3 grid, 500 steps, and a 100,000-sphere version of it):
 * one 500-step fcdemUpdate call (the state kept in sorted order between
   steps) ends in exactly the state of 500 single-step calls;
 * trajectories are chaotic, so a 100-step run is compared with the oracle's
-  by total kinetic and potential energy, momentum and contact count; the
-  same for 60 steps of the unified-memory step (evalForces, integrate with
-  the torus distance map, the cylinder and the planes) of the torus fall."""
+  (host arithmetic, every product rounded) by total kinetic and potential
+  energy, momentum and contact count, and with the oracle in the GPU's
+  fused arithmetic, whose run has the same statistics exactly; the same
+  comparison by statistics for 60 steps of the unified-memory step
+  (evalForces, integrate with the torus distance map, the cylinder and the
+  planes) of the torus fall."""
 import numpy as np
 import pytest
 import torch
@@ -86,10 +89,19 @@ def test_packed_multistep_statistics_match_oracle():
     o = _stats(pos, vel, P, True)
     print(f"GPU ke {g[0]:.6e} pe {g[1]:.6e} contacts {g[3]}; "
           f"oracle ke {o[0]:.6e} pe {o[1]:.6e} contacts {o[3]}")
+    # the host arithmetic rounds every product, the GPU fuses them: over 100
+    # steps of the hot packing the trajectories part (chaos), and the
+    # contact count, a count of near-threshold pairs, moves by a few percent
     assert abs(g[0] - o[0]) <= 0.02 * o[0]
     assert abs(g[1] - o[1]) <= 1e-3 * abs(o[1])
     assert np.all(np.abs(g[2] - o[2]) <= 0.05 * np.abs(o[2]).max() + 1e-9)
-    assert abs(g[3] - o[3]) <= 0.02 * o[3]
+    assert abs(g[3] - o[3]) <= 0.04 * o[3]
+    # with the GPU's fused arithmetic the oracle's run has the same statistics
+    pos, vel = sc["pos"].copy(), sc["vel"].copy()
+    with O.gpu_arithmetic():
+        O.update(P, pos, vel, sc["dt"], steps=steps, radius_from_w=True)
+    f = _stats(pos, vel, P, True)
+    assert f[0] == g[0] and f[1] == g[1] and f[3] == g[3]
 
 
 def test_um_torus_fall_statistics_match_oracle():
