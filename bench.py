@@ -517,6 +517,35 @@ def measure_torus_obstacle(n: int, steps: int, dev: int) -> dict:
         del us
     same = all(torch.equal(a.view(torch.int32), b.view(torch.int32))
                for a, b in zip(finals["plain"], finals["neural"]))
+    # The same scene over finer analytic maps of the torus (the map grows
+    # past the 129 MB L2): what an exact query costs against the network as
+    # the map leaves the cache.  The network is the one trained above.
+    curve = []
+    for cpa in (128, 256, 512, 768):
+        big = dem.DistanceMap.torus(0.3, 0.1, cpa, 0.05)
+        row = {"cells_per_axis": cpa, "map_mb": float(np.prod(np.array(big.cells) + 1)) * 16 / 1e6}
+        res = {}
+        for mode in ("exact", "neural"):
+            us = dem.UmScene(sc, big, f"cuda:{dev}")
+            kw = dict(net=net, skin=skin) if mode == "neural" else {}
+            us.update(3, **kw)
+            us.pos.copy_(torch.from_numpy(sc["pos"]))
+            us.vel.copy_(torch.from_numpy(sc["vel"]))
+            torch.cuda.synchronize()
+            e0.record()
+            us.update(100, force=False, **kw)
+            e1.record()
+            torch.cuda.synchronize()
+            dem.check(f"map curve {cpa} {mode}")
+            row[f"{mode}_ms_per_step"] = e0.elapsed_time(e1) / 100
+            res[mode] = (us.pos.clone(), us.vel.clone())
+            del us
+        row["neural_over_exact"] = row["exact_ms_per_step"] / row["neural_ms_per_step"]
+        row["equal_final_state"] = all(torch.equal(a.view(torch.int32), b.view(torch.int32))
+                                       for a, b in zip(res["exact"], res["neural"]))
+        curve.append(row)
+        del big, res
+        torch.cuda.empty_cache()
     return {"workload": f"{n} spheres r=1/256 falling onto a torus (R 0.3, r 0.1; mesh of "
                         "256 x 64 quads, 32768 triangles), 128-cell distance map built from the "
                         "mesh on the GPU, unified-memory step (calcHash, sort, reorder, "
@@ -526,6 +555,8 @@ def measure_torus_obstacle(n: int, steps: int, dev: int) -> dict:
             "plain_exact_map": out["plain"], "neural_sdf": out["neural"],
             "speedup": out["neural"]["value"] / out["plain"]["value"],
             "equal_final_state": bool(same),
+            "map_size_curve": {"steps": 100, "maps": "analytic torus maps, 16 B per vertex",
+                               "points": curve},
             "network": {"layers": "3-64-64-64-1 SiLU", "params": net.num_params,
                         "train_samples": 2_000_000, "epochs": 20, "train_s": train_s,
                         "final_loss": loss, "judge": judge},
