@@ -783,39 +783,36 @@ kCollideTiled(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
 // ---------------------------------------------------------------------------
 // Warp-cooperative collide over the prefix cell table (linear cell order).
 //
-// The lanes of a warp hold 32 consecutive sorted particles.  For each of the
-// nine neighbour rows every particle has one range of candidate partners
-// (the row's three cells are consecutive hashes when x does not wrap).  The
-// (particle, partner) pairs of the warp's 32 ranges are cut into 32 chunks
-// of equal length, one per lane, so that every lane tests as many
-// candidates as any other, whatever the spread of the ranges; a lane walks
-// its chunk in (particle, partner) order and moves to the next particle's
-// range when it reaches its end.  A candidate below the squared-distance
-// bound (rejectBound) goes to its particle's list of near partners in
-// shared memory, keyed by (neighbour cell, sorted index).  After the nine
-// rows each lane sorts its own particle's list -- which is then in the
-// reference's order: cells in z, y, x order, partners in ascending sorted
-// index -- and runs the exact test and the contact terms in that order,
-// with the cell subtotals of collideCell (particles_kernel.cu:223-285).  The
-// sums are kCollideGlobal's bit for bit.
+// The lanes of a warp hold 32 consecutive sorted particles.  Each particle
+// has nine candidate ranges, one per neighbour row (the row's three cells
+// are consecutive hashes when x does not wrap; culling trims them).  The
+// warp's candidate pairs -- particle by particle, row by row, partner by
+// partner -- form one sequence, cut into 32 chunks of equal length, one per
+// lane: every lane tests as many candidates as any other, whatever the
+// spread of the particles' neighbourhoods, and no lane waits at a row
+// boundary.  A candidate below the squared-distance bound (rejectBound)
+// goes to its particle's list of near partners in shared memory, keyed by
+// (neighbour cell, sorted index).  Then each lane sorts its own particle's
+// list -- which puts it in the reference's order: cells in z, y, x order,
+// partners in ascending sorted index -- and runs the exact test and the
+// contact terms in that order, with the cell subtotals of collideCell
+// (particles_kernel.cu:223-285).  The sums are kCollideGlobal's bit for bit.
 //
-// A particle whose row would wrap in x, or whose list overflows, is handed
+// A particle whose rows would wrap in x, or whose list overflows, is handed
 // to kCollideCrowd as a group of one (that kernel walks any particle's 27
 // cells in the reference's order); a particle in a crowded neighbourhood is
-// deferred there as in kCollideGlobal.
+// deferred there with its cell, as in kCollideGlobal.
 constexpr int kWarpWarps = 4;            // warps per CTA
-constexpr int kListCap = 32;             // near partners per particle
-constexpr int kWarpStage = 160;          // staged partner positions per warp and row
+constexpr int kListCap = 24;             // near partners per particle
 constexpr unsigned kKeyCellShift = 27;   // list key: neighbour cell << 27 | sorted index
 constexpr unsigned kKeyIndexMask = (1u << kKeyCellShift) - 1u;
 
 struct __align__(16) WarpSmem {
-  float4 stage[kWarpStage];      // the row's partners, when their union is short
+  uint4 row[9][32];              // per row and lane: range start, end, cell bounds o1, o2
   float4 me[32];                 // each lane's particle: x, y, z, radius
   unsigned list[kListCap][32];   // [entry][lane]: one bank per lane
   unsigned count[32];
-  unsigned pre[33];              // exclusive prefix of the row's range lengths
-  unsigned a[32], o1[32], o2[32];  // range start; its cell boundaries
+  unsigned pre[33];              // exclusive prefix of the lanes' pair counts
 };
 
 __device__ __forceinline__ void deferOne(const CrowdList &crowd, unsigned i) {
@@ -843,8 +840,43 @@ kCollideWarp(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
   const float3 pos = make_float3(p4.x, p4.y, p4.z), vel = make_float3(v4.x, v4.y, v4.z);
   const float ri = kRadiusFromW ? p4.w : P.particleRadius;
   const int3 g = gridPos(pos.x, pos.y, pos.z, P);
+  bool lcull = cull;
+  if (valid && kRadiusFromW && !(ri <= P.particleRadius)) {
+    atomicOr(status, (unsigned)kStatusRadiusBound);
+    lcull = false;
+  }
+  const unsigned gxm = P.gridSize[0] - 1u;
+  const unsigned xm = (unsigned)g.x & gxm;
+  const bool merged = xm >= 1u && xm < gxm;
   bool mine = valid;  // this kernel finishes the particle
-  if (mine && neighbourhoodCount<true>(g, cells, n, P) > crowd.limit) {
+  bool scan = valid && merged && !inertPos(pos);
+  const CellCull cc = makeCull(pos, g, ri + P.particleRadius, P);
+  const float cullR2 = lcull ? cc.r2 : __int_as_float(0x7f800000);
+  // The nine rows: culled ranges, and the whole rows for the crowd test.
+  unsigned total = 0u, hood = 0u;
+#pragma unroll
+  for (int row = 0; row < 9; row++) {
+    const int z = row / 3 - 1, y = row % 3 - 1;
+    uint4 r = make_uint4(0u, 0u, 0u, 0u);
+    if (valid && merged) {
+      const unsigned h0 = gridHash(g.x - 1, g.y + y, g.z + z, P);
+      const unsigned q0 = __ldg(cells.off + h0), q1 = __ldg(cells.off + h0 + 1);
+      const unsigned q2 = __ldg(cells.off + h0 + 2), q3 = __ldg(cells.off + h0 + 3);
+      hood += q3 > q0 ? q3 - q0 : 0u;
+      const float rowD2 = CellCull::pick(z, cc.zl, cc.zh) + CellCull::pick(y, cc.yl, cc.yh);
+      if (scan && rowD2 <= cullR2) {
+        r.x = rowD2 + cc.xl <= cullR2 ? q0 : q1;
+        r.y = min(rowD2 + cc.xh <= cullR2 ? q3 : q2, n);
+        if (r.y < r.x) r.y = r.x;
+        r.z = q1;
+        r.w = q2;
+      }
+    }
+    sm.row[row][lane] = r;
+    total += r.y - r.x;
+  }
+  if (valid && !merged) hood = neighbourhoodCount<true>(g, cells, n, P);
+  if (valid && hood > crowd.limit) {
     unsigned a, b;
     cellRange<true>(gridHash(g.x, g.y, g.z, P), cells, n, a, b);
     if (i >= a && i < b) {  // deferred to kCollideCrowd with its cell's members
@@ -853,108 +885,75 @@ kCollideWarp(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
         if (k < crowd.cap) crowd.groups[k] = make_uint2(i, min(32u, b - i));
       }
       mine = false;
+      scan = false;
+      total = 0u;
     }
   }
-  bool lcull = cull;
-  if (mine && kRadiusFromW && !(ri <= P.particleRadius)) {
-    atomicOr(status, (unsigned)kStatusRadiusBound);
-    lcull = false;
-  }
-  const unsigned gxm = P.gridSize[0] - 1u;
-  const unsigned xm = (unsigned)g.x & gxm;
-  if (mine && !inertPos(pos) && !(xm >= 1u && xm < gxm)) {  // the row wraps in x
+  if (mine && !merged && !inertPos(pos)) {  // its rows wrap in x
     deferOne(crowd, i);
     mine = false;
   }
-  // an inert particle's force is +0.0 (inertPos): it scans nothing
-  const bool scan = mine && !inertPos(pos);
-  const float cdMono = ri + P.particleRadius;
-  const float cdMonoHi2 = rejectBound(cdMono);
-  const CellCull cc = makeCull(pos, g, ri + P.particleRadius, P);
-  const float cullR2 = lcull ? cc.r2 : __int_as_float(0x7f800000);
+  if (!scan) {  // nothing to walk: empty rows (a deferred particle's were filled)
+    total = 0u;
+#pragma unroll
+    for (int row = 0; row < 9; row++) sm.row[row][lane] = make_uint4(0u, 0u, 0u, 0u);
+  }
   sm.me[lane] = make_float4(pos.x, pos.y, pos.z, ri);
   sm.count[lane] = 0u;
-  __syncwarp();
-#pragma unroll 1
-  for (int row = 0; row < 9; row++) {
-    const int z = row / 3 - 1, y = row % 3 - 1;
-    unsigned a = 0u, b = 0u, o1 = 0u, o2 = 0u;
-    if (scan) {
-      const float rowD2 = CellCull::pick(z, cc.zl, cc.zh) + CellCull::pick(y, cc.yl, cc.yh);
-      if (rowD2 <= cullR2) {
-        const bool useL = rowD2 + cc.xl <= cullR2;
-        const bool useR = rowD2 + cc.xh <= cullR2;
-        const unsigned h0 = gridHash(g.x - 1, g.y + y, g.z + z, P);
-        const unsigned q0 = __ldg(cells.off + h0);
-        o1 = __ldg(cells.off + h0 + 1);
-        o2 = __ldg(cells.off + h0 + 2);
-        const unsigned q3 = __ldg(cells.off + h0 + 3);
-        a = useL ? q0 : o1;
-        b = min(useR ? q3 : o2, n);
-        if (b < a) b = a;
-      }
-    }
-    const unsigned len = b - a;
-    unsigned incl = len;
+  unsigned incl = total;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
-      if ((int)lane >= o) incl += t;
-    }
-    const unsigned total = __shfl_sync(0xffffffffu, incl, 31);
-    if (total == 0u) continue;  // warp-uniform
-    sm.pre[lane + 1] = incl;
-    if (lane == 0) sm.pre[0] = 0u;
-    sm.a[lane] = a;
-    sm.o1[lane] = o1;
-    sm.o2[lane] = o2;
-    // The lanes' ranges mostly overlap (consecutive particles, mostly one
-    // grid row): their union is copied to shared memory with coalesced
-    // loads when it is short.
-    const unsigned lo = __reduce_min_sync(0xffffffffu, len ? a : 0xffffffffu);
-    const unsigned hi = __reduce_max_sync(0xffffffffu, len ? b : 0u);
-    const bool staged = hi - lo <= (unsigned)kWarpStage;
-    if (staged)
-      for (unsigned t = lane; t < hi - lo; t += 32u) sm.stage[t] = ldg4(sortedPos + lo + t);
-    __syncwarp();
-    const unsigned chunk = (total + 31u) >> 5;
-    unsigned k = lane * chunk;
-    const unsigned kEnd = min(k + chunk, total);
-    if (k < kEnd) {
-      // the particle whose range holds pair k: the last il with pre[il] <= k
-      // (pre[32] = total > k, so il <= 31 and pre[il + 1] > k)
-      unsigned il = 0u;
-#pragma unroll
-      for (unsigned st = 16u; st; st >>= 1)
-        if (sm.pre[il + st] <= k) il += st;
-      float4 me = sm.me[il];
-      unsigned next = sm.pre[il + 1];
-      unsigned j = sm.a[il] + (k - sm.pre[il]);
-      unsigned m1 = sm.o1[il], m2 = sm.o2[il];
-      for (; k < kEnd; ++k, ++j) {
-        if (k == next) {  // the next particle with a non-empty range
-          do {
-            ++il;
-            next = sm.pre[il + 1];
-          } while (next == k);
-          me = sm.me[il];
-          j = sm.a[il];
-          m1 = sm.o1[il];
-          m2 = sm.o2[il];
-        }
-        const float4 q4 = staged ? sm.stage[j - lo] : ldg4(sortedPos + j);
-        const float3 rel = make_float3(q4.x - me.x, q4.y - me.y, q4.z - me.z);
-        const float d2 = pairDist2(rel);
-        const float hi2 = kRadiusFromW ? rejectBound(me.w + q4.w) : cdMonoHi2;
-        if (d2 < hi2) {  // the particle itself too (d2 = 0): skipped in the drain
-          const unsigned cell = (unsigned)row * 3u + (j >= m1) + (j >= m2);
-          const unsigned slot = atomicAdd(&sm.count[il], 1u);
-          if (slot < (unsigned)kListCap) sm.list[slot][il] = (cell << kKeyCellShift) | j;
-        }
-      }
-    }
-    __syncwarp();  // the staged rows and range arrays are reused by the next row
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+    if ((int)lane >= o) incl += t;
   }
+  sm.pre[lane + 1] = incl;
+  if (lane == 0) sm.pre[0] = 0u;
+  const unsigned all = __shfl_sync(0xffffffffu, incl, 31);
+  __syncwarp();
+  const float cdMonoHi2 = rejectBound(ri + P.particleRadius);  // uniform when monodisperse
+  const unsigned chunk = (all + 31u) >> 5;
+  unsigned k = lane * chunk;
+  const unsigned kEnd = min(k + chunk, all);
+  if (k < kEnd) {
+    // the particle holding pair k: the last il with pre[il] <= k (pre[32] =
+    // all > k, so il <= 31 and pre[il + 1] > k); then its row
+    unsigned il = 0u;
+#pragma unroll
+    for (unsigned st = 16u; st; st >>= 1)
+      if (sm.pre[il + st] <= k) il += st;
+    unsigned off = k - sm.pre[il];
+    int row = 0;
+    uint4 r = sm.row[0][il];
+    while (off >= r.y - r.x) {
+      off -= r.y - r.x;
+      r = sm.row[++row][il];
+    }
+    float4 me = sm.me[il];
+    unsigned j = r.x + off;
+    for (; k < kEnd; ++k, ++j) {
+      if (j == r.y) {  // the next non-empty row, of this particle or a later one
+        do {
+          if (++row == 9) {
+            row = 0;
+            ++il;
+            me = sm.me[il];
+          }
+          r = sm.row[row][il];
+        } while (r.x == r.y);
+        j = r.x;
+      }
+      const float4 q4 = ldg4(sortedPos + j);
+      const float3 rel = make_float3(q4.x - me.x, q4.y - me.y, q4.z - me.z);
+      const float d2 = pairDist2(rel);
+      const float hi2 = kRadiusFromW ? rejectBound(me.w + q4.w) : cdMonoHi2;
+      if (d2 < hi2) {  // the particle itself too (d2 = 0): skipped in the drain
+        const unsigned cell = (unsigned)row * 3u + (j >= r.z) + (j >= r.w);
+        const unsigned slot = atomicAdd(&sm.count[il], 1u);
+        if (slot < (unsigned)kListCap) sm.list[slot][il] = (cell << kKeyCellShift) | j;
+      }
+    }
+  }
+  __syncwarp();
   if (!mine) return;
   float3 force = make_float3(0.0f, 0.0f, 0.0f);
   if (scan) {
@@ -966,13 +965,14 @@ kCollideWarp(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
     // insertion sort: (cell, sorted index) ascending is the reference's order
     for (unsigned t = 1; t < c; ++t) {
       const unsigned key = sm.list[t][lane];
-      unsigned s = t;
-      while (s > 0u && sm.list[s - 1][lane] > key) {
-        sm.list[s][lane] = sm.list[s - 1][lane];
-        --s;
+      unsigned s2 = t;
+      while (s2 > 0u && sm.list[s2 - 1][lane] > key) {
+        sm.list[s2][lane] = sm.list[s2 - 1][lane];
+        --s2;
       }
-      sm.list[s][lane] = key;
+      sm.list[s2][lane] = key;
     }
+    const float cdMono = ri + P.particleRadius;
     float3 cf = make_float3(0.0f, 0.0f, 0.0f);
     int cfCell = -1;
     for (unsigned t = 0; t < c; ++t) {
