@@ -31,6 +31,7 @@ struct fcdemBatch {
   const void *gPos = nullptr, *gVel = nullptr;
   float gDt = 0.0f;
   unsigned gSteps = 0;
+  unsigned gNetVersion = 0;  // the network's version when the graph was recorded
   // obstacles (fcdemBatchSetObstacles)
   std::vector<fcdem::BatchScene> hostScenes;
   fcdem::MapView *maps = nullptr;  // device, one per shape
@@ -268,8 +269,10 @@ void fcdemBatchUpdate(fcdemBatch *b, float *pos, float *vel, float deltaTime, ui
     runBatch(b, (float4 *)pos, (float4 *)vel, deltaTime, steps);
     return;
   }
+  // the network's normalisation and BF16 weights are recorded by value: a
+  // retrained network needs a new recording
   const bool same = b->exec && b->gPos == pos && b->gVel == vel && b->gDt == deltaTime &&
-                    b->gSteps == steps;
+                    b->gSteps == steps && (!b->net || sdfVersion(b->net) == b->gNetVersion);
   if (!same) {
     if (b->exec) {
       cudaGraphExecDestroy(b->exec);
@@ -299,6 +302,7 @@ void fcdemBatchUpdate(fcdemBatch *b, float *pos, float *vel, float deltaTime, ui
     b->gVel = vel;
     b->gDt = deltaTime;
     b->gSteps = steps;
+    b->gNetVersion = sdfVersion(b->net);
   }
   cudaOk(cudaGraphLaunch(b->exec, curStream()));
 }

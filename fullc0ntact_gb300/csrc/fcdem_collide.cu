@@ -781,56 +781,38 @@ kCollideTiled(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
 }
 
 // ---------------------------------------------------------------------------
-// Warp-cooperative collide over the prefix cell table (linear cell order).
+// Collide with one flattened candidate loop per thread (prefix cell table,
+// linear cell order).
 //
-// The lanes of a warp hold 32 consecutive sorted particles.  Each particle
-// has nine candidate ranges, one per neighbour row (the row's three cells
-// are consecutive hashes when x does not wrap; culling trims them).  The
-// warp's candidate pairs -- particle by particle, row by row, partner by
-// partner -- form one sequence, cut into 32 chunks of equal length, one per
-// lane: every lane tests as many candidates as any other, whatever the
-// spread of the particles' neighbourhoods, and no lane waits at a row
-// boundary.  A candidate below the squared-distance bound (rejectBound)
-// goes to its particle's list of near partners in shared memory, keyed by
-// (neighbour cell, sorted index).  Then each lane sorts its own particle's
-// list -- which puts it in the reference's order: cells in z, y, x order,
-// partners in ascending sorted index -- and runs the exact test and the
-// contact terms in that order, with the cell subtotals of collideCell
-// (particles_kernel.cu:223-285).  The sums are kCollideGlobal's bit for bit.
-//
-// A particle whose rows would wrap in x, or whose list overflows, is handed
-// to kCollideCrowd as a group of one (that kernel walks any particle's 27
-// cells in the reference's order); a particle in a crowded neighbourhood is
-// deferred there with its cell, as in kCollideGlobal.
-constexpr int kWarpWarps = 4;            // warps per CTA
-constexpr int kListCap = 24;             // near partners per particle
-constexpr unsigned kKeyCellShift = 27;   // list key: neighbour cell << 27 | sorted index
-constexpr unsigned kKeyIndexMask = (1u << kKeyCellShift) - 1u;
-
-struct __align__(16) WarpSmem {
-  uint4 row[9][32];              // per row and lane: range start, end, cell bounds o1, o2
-  float4 me[32];                 // each lane's particle: x, y, z, radius
-  unsigned list[kListCap][32];   // [entry][lane]: one bank per lane
-  unsigned count[32];
-  unsigned pre[33];              // exclusive prefix of the lanes' pair counts
-};
-
-__device__ __forceinline__ void deferOne(const CrowdList &crowd, unsigned i) {
-  const unsigned k = atomicAdd(crowd.count, 1u);
-  if (k < crowd.cap) crowd.groups[k] = make_uint2(i, 1u);
-}
+// kCollideGlobal walks the nine neighbour rows one after the other, and the
+// lanes of a warp meet at the end of every row: a row costs the warp its
+// longest lane's range.  Here each thread first computes all nine ranges
+// (the table loads of all rows in flight together), the warp copies the
+// union of its lanes' ranges of every row that fits into shared memory, and
+// then each thread walks its nine ranges as one sequence in a single loop:
+// the warp costs its longest lane's whole neighbourhood, not the sum of nine
+// row maxima.  The candidate test, the near-partner queue and its drain are
+// kCollideGlobal's, so the sums are the same bits.  A particle whose rows
+// wrap in x, or with a row range above 1023 candidates, takes kCollideGlobal's
+// per-cell loop; crowded neighbourhoods are deferred to kCollideCrowd.
+constexpr int kFlatStage = 256;            // staged partner positions per warp
+constexpr unsigned kFlatLenMask = 1023u;   // row word: len | (o1 - a) << 10 | (o2 - a) << 20
+constexpr int kNotStaged = -2147483647 - 1;
 
 template <int kMode, bool kRadiusFromW, bool kCollider, bool kForceOut>
-__global__ void __launch_bounds__(kWarpWarps * 32)
-kCollideWarp(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
+__global__ void __launch_bounds__(128)
+kCollideFlat(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
              const float4 *__restrict__ sortedVel, const unsigned *__restrict__ index,
              CellRanges cells, unsigned n, KParams kp, CollideOut out, bool cull,
              CrowdList crowd, unsigned *status) {
-  __shared__ WarpSmem smAll[kWarpWarps];
+  __shared__ uint2 sRow[9][128];              // per row and thread: start, row word
+  __shared__ float4 sStage[4][kFlatStage];    // per warp: the staged rows
+  __shared__ int sDelta[4][9];                // stage index - sorted index, or kNotStaged
+  __shared__ unsigned qj[kQueueLen * kQueueStride];
+  __shared__ unsigned char qc[kQueueLen * kQueueStride];
   const SimParams &P = kp.p;
-  const unsigned lane = threadIdx.x & 31u;
-  WarpSmem &sm = smAll[threadIdx.x >> 5];
-  const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const unsigned i = blockIdx.x * blockDim.x + tid;
   const bool valid = i < n;
   float4 p4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), v4 = p4;
   if (valid) {
@@ -848,35 +830,37 @@ kCollideWarp(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
   const unsigned gxm = P.gridSize[0] - 1u;
   const unsigned xm = (unsigned)g.x & gxm;
   const bool merged = xm >= 1u && xm < gxm;
-  bool mine = valid;  // this kernel finishes the particle
-  bool scan = valid && merged && !inertPos(pos);
+  const bool inert = inertPos(pos);  // an inert particle's force is +0.0
+  bool flat = valid && merged && !inert;
   const CellCull cc = makeCull(pos, g, ri + P.particleRadius, P);
   const float cullR2 = lcull ? cc.r2 : __int_as_float(0x7f800000);
-  // The nine rows: culled ranges, and the whole rows for the crowd test.
-  unsigned total = 0u, hood = 0u;
+  unsigned hood = 0u;
 #pragma unroll
   for (int row = 0; row < 9; row++) {
     const int z = row / 3 - 1, y = row % 3 - 1;
-    uint4 r = make_uint4(0u, 0u, 0u, 0u);
+    uint2 e = make_uint2(0u, 0u);
     if (valid && merged) {
       const unsigned h0 = gridHash(g.x - 1, g.y + y, g.z + z, P);
       const unsigned q0 = __ldg(cells.off + h0), q1 = __ldg(cells.off + h0 + 1);
       const unsigned q2 = __ldg(cells.off + h0 + 2), q3 = __ldg(cells.off + h0 + 3);
       hood += q3 > q0 ? q3 - q0 : 0u;
       const float rowD2 = CellCull::pick(z, cc.zl, cc.zh) + CellCull::pick(y, cc.yl, cc.yh);
-      if (scan && rowD2 <= cullR2) {
-        r.x = rowD2 + cc.xl <= cullR2 ? q0 : q1;
-        r.y = min(rowD2 + cc.xh <= cullR2 ? q3 : q2, n);
-        if (r.y < r.x) r.y = r.x;
-        r.z = q1;
-        r.w = q2;
+      if (rowD2 <= cullR2) {
+        const unsigned a = rowD2 + cc.xl <= cullR2 ? q0 : q1;
+        unsigned b = min(rowD2 + cc.xh <= cullR2 ? q3 : q2, n);
+        if (b < a) b = a;
+        const unsigned len = b - a;
+        if (len > kFlatLenMask) flat = false;  // too long for the row word
+        const unsigned d1 = q1 > a ? min(q1 - a, kFlatLenMask) : 0u;
+        const unsigned d2 = q2 > a ? min(q2 - a, kFlatLenMask) : 0u;
+        e = make_uint2(a, min(len, kFlatLenMask) | (d1 << 10) | (d2 << 20));
       }
     }
-    sm.row[row][lane] = r;
-    total += r.y - r.x;
+    sRow[row][tid] = e;
   }
+  bool mine = valid;
   if (valid && !merged) hood = neighbourhoodCount<true>(g, cells, n, P);
-  if (valid && hood > crowd.limit) {
+  if (valid && crowd.groups && hood > crowd.limit) {
     unsigned a, b;
     cellRange<true>(gridHash(g.x, g.y, g.z, P), cells, n, a, b);
     if (i >= a && i < b) {  // deferred to kCollideCrowd with its cell's members
@@ -885,127 +869,110 @@ kCollideWarp(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
         if (k < crowd.cap) crowd.groups[k] = make_uint2(i, min(32u, b - i));
       }
       mine = false;
-      scan = false;
-      total = 0u;
+      flat = false;
     }
   }
-  if (mine && !merged && !inertPos(pos)) {  // its rows wrap in x
-    deferOne(crowd, i);
-    mine = false;
-  }
-  if (!scan) {  // nothing to walk: empty rows (a deferred particle's were filled)
-    total = 0u;
+  if (!flat) {  // no rows to walk (and none to stage for this thread)
 #pragma unroll
-    for (int row = 0; row < 9; row++) sm.row[row][lane] = make_uint4(0u, 0u, 0u, 0u);
-  }
-  sm.me[lane] = make_float4(pos.x, pos.y, pos.z, ri);
-  sm.count[lane] = 0u;
-  unsigned incl = total;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
-    if ((int)lane >= o) incl += t;
-  }
-  sm.pre[lane + 1] = incl;
-  if (lane == 0) sm.pre[0] = 0u;
-  const unsigned all = __shfl_sync(0xffffffffu, incl, 31);
-  __syncwarp();
-  const float cdMonoHi2 = rejectBound(ri + P.particleRadius);  // uniform when monodisperse
-  const unsigned chunk = (all + 31u) >> 5;
-  unsigned k = lane * chunk;
-  const unsigned kEnd = min(k + chunk, all);
-  if (k < kEnd) {
-    // the particle holding pair k: the last il with pre[il] <= k (pre[32] =
-    // all > k, so il <= 31 and pre[il + 1] > k); then its row
-    unsigned il = 0u;
-#pragma unroll
-    for (unsigned st = 16u; st; st >>= 1)
-      if (sm.pre[il + st] <= k) il += st;
-    unsigned off = k - sm.pre[il];
-    int row = 0;
-    uint4 r = sm.row[0][il];
-    while (off >= r.y - r.x) {
-      off -= r.y - r.x;
-      r = sm.row[++row][il];
-    }
-    float4 me = sm.me[il];
-    unsigned j = r.x + off;
-    for (; k < kEnd; ++k, ++j) {
-      if (j == r.y) {  // the next non-empty row, of this particle or a later one
-        do {
-          if (++row == 9) {
-            row = 0;
-            ++il;
-            me = sm.me[il];
-          }
-          r = sm.row[row][il];
-        } while (r.x == r.y);
-        j = r.x;
-      }
-      const float4 q4 = ldg4(sortedPos + j);
-      const float3 rel = make_float3(q4.x - me.x, q4.y - me.y, q4.z - me.z);
-      const float d2 = pairDist2(rel);
-      const float hi2 = kRadiusFromW ? rejectBound(me.w + q4.w) : cdMonoHi2;
-      if (d2 < hi2) {  // the particle itself too (d2 = 0): skipped in the drain
-        const unsigned cell = (unsigned)row * 3u + (j >= r.z) + (j >= r.w);
-        const unsigned slot = atomicAdd(&sm.count[il], 1u);
-        if (slot < (unsigned)kListCap) sm.list[slot][il] = (cell << kKeyCellShift) | j;
-      }
-    }
+    for (int row = 0; row < 9; row++) sRow[row][tid] = make_uint2(0u, 0u);
   }
   __syncwarp();
-  if (!mine) return;
+  // The union of the warp's ranges of each row, staged while they fit.
+  unsigned seg = 0u;
+#pragma unroll 1
+  for (int row = 0; row < 9; row++) {
+    const uint2 e = sRow[row][tid];
+    const unsigned len = e.y & kFlatLenMask;
+    const unsigned lo = __reduce_min_sync(0xffffffffu, len ? e.x : 0xffffffffu);
+    const unsigned hi = __reduce_max_sync(0xffffffffu, len ? e.x + len : 0u);
+    int delta = kNotStaged;
+    if (lo < hi && seg + (hi - lo) <= (unsigned)kFlatStage) {
+      for (unsigned t = lane; t < hi - lo; t += 32u) sStage[warp][seg + t] = ldg4(sortedPos + lo + t);
+      delta = (int)seg - (int)lo;
+      seg += hi - lo;
+    }
+    if (lane == 0) sDelta[warp][row] = delta;
+  }
+  __syncwarp();
   float3 force = make_float3(0.0f, 0.0f, 0.0f);
-  if (scan) {
-    const unsigned c = sm.count[lane];
-    if (c > (unsigned)kListCap) {  // more near partners than the list holds
-      deferOne(crowd, i);
-      return;
-    }
-    // insertion sort: (cell, sorted index) ascending is the reference's order
-    for (unsigned t = 1; t < c; ++t) {
-      const unsigned key = sm.list[t][lane];
-      unsigned s2 = t;
-      while (s2 > 0u && sm.list[s2 - 1][lane] > key) {
-        sm.list[s2][lane] = sm.list[s2 - 1][lane];
-        --s2;
-      }
-      sm.list[s2][lane] = key;
-    }
+  if (flat) {
     const float cdMono = ri + P.particleRadius;
+    const float cdMonoHi2 = rejectBound(cdMono);
+    unsigned *qjT = qj + tid;
+    unsigned char *qcT = qc + tid;
     float3 cf = make_float3(0.0f, 0.0f, 0.0f);
     int cfCell = -1;
-    for (unsigned t = 0; t < c; ++t) {
-      const unsigned key = sm.list[t][lane];
-      const unsigned j = key & kKeyIndexMask;
-      if (j == i) continue;
-      const int cell = (int)(key >> kKeyCellShift);
-      const float4 q4 = ldg4(sortedPos + j);
-      const float3 rel = make_float3(q4.x - pos.x, q4.y - pos.y, q4.z - pos.z);
-      const float dist = sqrtf(pairDist2(rel));
-      const float cd = kRadiusFromW ? ri + q4.w : cdMono;
-      if (dist < cd) {
-        if (cell != cfCell) {
-          force.x = force.x + cf.x;
-          force.y = force.y + cf.y;
-          force.z = force.z + cf.z;
-          cf = make_float3(0.0f, 0.0f, 0.0f);
-          cfCell = cell;
+    int qn = 0;
+    auto drain = [&]() {
+      for (int q = 0; q < qn; ++q) {
+        const unsigned j = qjT[q * kQueueStride];
+        const int cell = qcT[q * kQueueStride];
+        const float4 q4 = ldg4(sortedPos + j);
+        const float3 rel = make_float3(q4.x - pos.x, q4.y - pos.y, q4.z - pos.z);
+        const float dist = sqrtf(pairDist2(rel));
+        const float cd = kRadiusFromW ? ri + q4.w : cdMono;
+        if (dist < cd) {
+          if (cell != cfCell) {
+            force.x = force.x + cf.x;
+            force.y = force.y + cf.y;
+            force.z = force.z + cf.z;
+            cf = make_float3(0.0f, 0.0f, 0.0f);
+            cfCell = cell;
+          }
+          const float4 w4 = ldg4(sortedVel + j);
+          const float3 f = contactTerm(rel, dist, cd, vel, make_float3(w4.x, w4.y, w4.z),
+                                       P.attraction, P);
+          cf.x = cf.x + f.x;
+          cf.y = cf.y + f.y;
+          cf.z = cf.z + f.z;
         }
-        const float4 w4 = ldg4(sortedVel + j);
-        const float3 f = contactTerm(rel, dist, cd, vel, make_float3(w4.x, w4.y, w4.z),
-                                     P.attraction, P);
-        cf.x = cf.x + f.x;
-        cf.y = cf.y + f.y;
-        cf.z = cf.z + f.z;
       }
+      qn = 0;
+    };
+    // one loop over the nine ranges: row switches are the only divergence
+    int row = -1;
+    unsigned j = 0u, end = 0u, a = 0u, word = 0u;
+    int delta = kNotStaged;
+    for (;;) {
+      if (j == end) {
+        uint2 e = make_uint2(0u, 0u);
+        do {
+          if (++row == 9) break;
+          e = sRow[row][tid];
+        } while ((e.y & kFlatLenMask) == 0u);
+        if (row == 9) break;
+        a = e.x;
+        word = e.y;
+        j = a;
+        end = a + (word & kFlatLenMask);
+        delta = sDelta[warp][row];
+      }
+      const float4 q4 = delta != kNotStaged ? sStage[warp][(int)j + delta] : ldg4(sortedPos + j);
+      const float3 rel = make_float3(q4.x - pos.x, q4.y - pos.y, q4.z - pos.z);
+      const float d2 = pairDist2(rel);
+      const float hi2 = kRadiusFromW ? rejectBound(ri + q4.w) : cdMonoHi2;
+      if (d2 < hi2 && j != i) {
+        if (qn == kQueueLen) drain();
+        const unsigned o = j - a;
+        qjT[qn * kQueueStride] = j;
+        qcT[qn * kQueueStride] =
+            (unsigned char)(row * 3 + (o >= ((word >> 10) & kFlatLenMask)) +
+                            (o >= ((word >> 20) & kFlatLenMask)));
+        ++qn;
+      }
+      ++j;
     }
+    drain();
     force.x = force.x + cf.x;
     force.y = force.y + cf.y;
     force.z = force.z + cf.z;
+  } else if (mine && !inert) {  // rows that wrap in x, or a row above the word's length
+    force = neighbourForceGlobal<kRadiusFromW, true>(i, n, pos, vel, ri, g, lcull, sortedPos,
+                                                     sortedVel, cells, P, qj + tid, qc + tid);
   }
-  finishParticle<kMode, kCollider, kForceOut>(i, n, pos, vel, p4, ri, force, index, newVel, out,
-                                              P);
+  if (mine)
+    finishParticle<kMode, kCollider, kForceOut>(i, n, pos, vel, p4, ri, force, index, newVel,
+                                                out, P);
 }
 
 bool g_crowdPath = true;  // fcdemSetCrowdPath
@@ -1047,22 +1014,17 @@ void launchT(bool tiled, bool warpPath, bool cull, unsigned n, float4 *newVel, c
     kCollideTiled<kMode, kRadiusFromW, kCollider, kForceOut>
         <<<blocks, kTileThreads, 0, curStream()>>>(newVel, sp, sv, index, cells, n, kp, out,
                                                    ctx().dStatus);
-  else if (kPrefix && warpPath && kp.p.maxParticlesPerCell != kMortonTag &&
-           n <= kKeyIndexMask) {
-    // the warp-cooperative kernel; its deferred particles (crowded, x-wrapping,
-    // list overflow) go to kCollideCrowd
-    CrowdList crowd = crowdList(n);
-    if (crowd.groups) {
-      kCollideWarp<kMode, kRadiusFromW, kCollider, kForceOut>
-          <<<(n + kWarpWarps * 32 - 1) / (kWarpWarps * 32), kWarpWarps * 32, 0, curStream()>>>(
+  else if (kPrefix && warpPath && kp.p.maxParticlesPerCell != kMortonTag) {
+    // the flattened-loop kernel; its crowded particles go to kCollideCrowd
+    const CrowdList crowd = crowdList(n);
+    kCollideFlat<kMode, kRadiusFromW, kCollider, kForceOut>
+        <<<blocks, 128, 0, curStream()>>>(newVel, sp, sv, index, cells, n, kp, out, cull, crowd,
+                                          ctx().dStatus);
+    if (crowd.groups && launchOk())
+      kCollideCrowd<kMode, kRadiusFromW, kCollider, kForceOut, kPrefix>
+          <<<numSms() * kCrowdCtasPerSm, kCrowdWarps * 32, 0, curStream()>>>(
               newVel, sp, sv, index, cells, n, kp, out, cull, crowd, ctx().dStatus);
-      if (launchOk())
-        kCollideCrowd<kMode, kRadiusFromW, kCollider, kForceOut, kPrefix>
-            <<<numSms() * kCrowdCtasPerSm, kCrowdWarps * 32, 0, curStream()>>>(
-                newVel, sp, sv, index, cells, n, kp, out, cull, crowd, ctx().dStatus);
-      return;
-    }
-    warpPath = false;  // no group list: the per-thread kernel covers every particle
+    return;
   }
   if (!(tiled && !kPrefix)) {
     const CrowdList crowd = crowdList(n);
@@ -1159,8 +1121,8 @@ void launchCollide(int mode, bool collider, float4 *newVel, const float4 *sp,
   // (its row windows assume the linear cell order)
   bool tiled = !prefix && g_collidePath == 1 && ((uintptr_t)sp & 15u) == 0 &&
                kp.p.maxParticlesPerCell != kMortonTag;
-  // the warp-cooperative kernel needs the prefix table and the group list
-  const bool warpPath = prefix && g_crowdPath && g_collidePath == 2;
+  // the flattened-loop kernel reads the prefix table
+  const bool warpPath = prefix && g_collidePath == 2;
   // Culling is exact when every grid dimension is >= 3 and the largest
   // contact distance 2 * particleRadius fits in the smallest cell.
   const SimParams &P = kp.p;

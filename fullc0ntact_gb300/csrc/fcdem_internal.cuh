@@ -232,6 +232,9 @@ bool batchObstacleIntegrate(const BatchScene *scenes, const unsigned *sceneOf, b
 // The network's per-tile culling hints for `tiles` tiles, allocated (and
 // cleared) when they grow; nullptr when they cannot be had.
 unsigned char *sdfHints(fcdemSdfNet *net, unsigned tiles);
+// Changes with every change of the network's weights or normalisation (a
+// recorded graph holds the values of its recording).
+unsigned sdfVersion(const fcdemSdfNet *net);
 // `step` (the step's number within a call) chooses the refresh steps of the
 // per-tile culling hints; -1: a lone call, no hints.
 bool sdfIntegrate(fcdemSdfNet *net, float4 *pos, float4 *vel, float dt, unsigned n,

@@ -843,6 +843,7 @@ struct fcdemSdfNet {
   __nv_bfloat16 *w16 = nullptr;
   bool w16Fresh = false;
   unsigned adamStep = 0;
+  unsigned version = 0;  // bumped whenever the weights or the normalisation change
   unsigned char *hints = nullptr;  // per-tile culling hints (TileHints)
   unsigned hintTiles = 0;
 };
@@ -896,6 +897,7 @@ bool uploadParams(fcdemSdfNet *net, const std::vector<float> &p) {
   const std::vector<float> t = transposed(net->lay, p);
   const size_t bytes = sizeof(float) * p.size();
   net->w16Fresh = false;
+  net->version++;
   return cudaOk(cudaMemcpy(net->params, p.data(), bytes, cudaMemcpyHostToDevice)) &&
          cudaOk(cudaMemcpy(net->paramsT, t.data(), bytes, cudaMemcpyHostToDevice));
 }
@@ -949,6 +951,7 @@ bool runTrainKernel(fcdemSdfNet *net, bool backward, const float4 *samples, cons
 bool adamStep(fcdemSdfNet *net, float lr) {
   const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
   net->adamStep++;
+  net->version++;
   const double t = (double)net->adamStep;
   const float c1 = (float)(1.0 / (1.0 - std::pow((double)b1, t)));
   const float c2 = (float)(1.0 / (1.0 - std::pow((double)b2, t)));
@@ -1057,6 +1060,8 @@ bool launchBatchObstacle(fcdemSdfNet *net, const BatchScene *scenes, const unsig
 }  // namespace fcdem
 
 namespace fcdem {
+
+unsigned sdfVersion(const fcdemSdfNet *net) { return net ? net->version : 0u; }
 
 // The net's hint array for `tiles` tiles (grown on demand, cleared when
 // grown); nullptr (no hints) when it cannot be had.
@@ -1207,6 +1212,7 @@ void fcdemSdfSetNormalization(fcdemSdfNet *net, const float shift[3], const floa
     net->scale[k] = scale[k];
   }
   net->outScale = outScale;
+  net->version++;
 }
 
 void fcdemSdfGetNormalization(const fcdemSdfNet *net, float shift[3], float scale[3],

@@ -225,8 +225,8 @@ void fcdemUpdate(float *pos, float *vel, float *sortedPos, float *sortedVel,
 
 /* Collide kernel selection: -1 (default) automatic, 0 the per-thread
  * global-read kernel, 1 the shared-memory tiled kernel (split cell tables),
- * 2 the warp-cooperative kernel (prefix cell table of fcdemUpdate and
- * fcdemUM_update).  All give identical results. */
+ * 2 the kernel with one flattened candidate loop per thread (prefix cell
+ * table of fcdemUpdate and fcdemUM_update).  All give identical results. */
 void fcdemSetCollidePath(int path);
 
 /* Test hook: the number of look-back rounds a tile of the radix sort
@@ -451,9 +451,10 @@ uint fcdemBatchNumParticles(const fcdemBatch *batch);
 uint fcdemBatchNumCells(const fcdemBatch *batch);
 /* `steps` updates of every scene, each stage one launch over all particles.
  * useGraph: the sequence is recorded as a CUDA graph on the first call (and
- * again when pos, vel, deltaTime or steps change) and replayed.  The result
- * equals `steps` ParticleSystem-style updates of each scene on its own (with
- * the scene's box). */
+ * again when pos, vel, deltaTime or steps change, or the obstacles' network
+ * has been trained or given new parameters or normalisation since) and
+ * replayed.  The result equals `steps` ParticleSystem-style updates of each
+ * scene on its own (with the scene's box). */
 void fcdemBatchUpdate(fcdemBatch *batch, float *pos, float *vel, float deltaTime, uint steps,
                       int useGraph);
 

@@ -92,3 +92,34 @@ def test_shape_network_judged_by_maps_and_culling_is_exact():
     ea, eb = a.exact_queries(), b.exact_queries()
     print("exact queries exact/neural", ea, eb)
     assert 0 < eb < 0.7 * ea, (ea, eb)
+
+
+def test_graph_records_again_after_the_network_changes():
+    """A batch replayed from a CUDA graph holds the network's normalisation
+    and BF16 weights of its recording; after the network is given new
+    parameters the next update records again.  Here the new parameters make
+    it predict a distance far above the skin everywhere, so the map queries
+    all but stop (the results then differ: the test is about the recording,
+    not about culling)."""
+    from fullc0ntact_gb300 import dem, sdf
+    scs, obs, shape = _small_obstacle_batch(num_scenes=3, n_min=3000, n_max=6000, seed=12)
+    maps = sdf.obstacle_maps(obs, 64)
+    net = sdf.SdfNet(3 + len(maps), 128, 2, seed=3)
+    net.set_normalization([0.0, 0.0, 0.0], [2.0, 2.0, 2.0], 0.5)
+    b = dem.Batch(scs)
+    b.set_obstacles(maps, shape, net=net, skin=10.0)  # nothing above the skin: no culling
+    b.update(30, graph=True)
+    b.update(10, graph=True)
+    b.exact_queries(reset=True)
+    b.update(10, graph=True)  # replay
+    dem.check("replay")
+    before = b.exact_queries(reset=True)
+    assert before > 0
+    p = np.zeros(net.num_params, np.float32)
+    p[-1] = 1e6  # output bias: every prediction far above the skin
+    net.set_params(p)
+    b.update(10, graph=True)
+    dem.check("after the change")
+    after = b.exact_queries(reset=True)
+    print("exact queries per 10 steps before / after", before, after)
+    assert after < 0.2 * before

@@ -1,6 +1,7 @@
 """The collide kernels give bit-identical results: the per-thread kernel with
 global reads, the kernel with shared-memory tiles staged by bulk copies, the
-warp-cooperative kernel, and the kernel for crowded neighbourhoods, on
+kernel with one flattened candidate loop per thread, and the kernel for
+crowded neighbourhoods, on
 scenes that exercise staged tiles, multi-row tiles, x-wrapping windows,
 crowded cells, inert particles and the polydisperse mode."""
 import numpy as np
@@ -235,12 +236,11 @@ def _run_path_update(sc, path, steps, um=False):
 
 @pytest.mark.parametrize("case", ["packed", "lattice", "wrap", "random_poly", "crowded",
                                   "inert", "torus_um"])
-def test_warp_kernel_equals_per_thread(case):
-    """The warp-cooperative collide (balanced chunks of candidate pairs,
-    per-particle lists of near partners sorted into the reference's order)
-    gives the per-thread kernel's bits: five fused updates, on scenes with
-    x-wrapping rows (handed to the crowded kernel one by one), crowded cells,
-    inert particles, and the unified-memory step's evalForces."""
+def test_flat_kernel_equals_per_thread(case):
+    """The collide with one flattened loop over the nine row ranges per
+    thread gives the per-row kernel's bits: five fused updates, on scenes
+    with x-wrapping rows (those particles take the per-cell loop), crowded
+    cells, inert particles, and the unified-memory step's evalForces."""
     from fullc0ntact_gb300 import scenes
     um = False
     if case == "packed":
@@ -263,11 +263,11 @@ def test_warp_kernel_equals_per_thread(case):
         np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
 
 
-def test_warp_kernel_list_overflow_is_exact():
-    """With the crowd limit raised, crowded cells go through the warp kernel,
-    whose near-partner lists (32 entries) overflow there: those particles are
-    handed to the crowded kernel one by one, and the results stay the
-    per-thread kernel's bits."""
+def test_flat_kernel_long_rows_are_exact():
+    """With the crowd limit raised, crowded cells go through the flattened
+    kernel, and their row ranges grow past the 1023 candidates its row word
+    holds: those particles take the per-cell loop, and the results stay the
+    per-row kernel's bits."""
     from fullc0ntact_gb300 import dem
     sc = _crowded_scene("packed")
     a = _run_path_update(sc, 0, 3)
