@@ -195,6 +195,7 @@ __device__ __forceinline__ float3 neighbourForceGlobal(
   auto drain = [&]() {
     for (int q = 0; q < qn; ++q) {
       const unsigned j = qj[q * kQueueStride];
+      if (j == i) continue;  // the scans queue the particle itself (d2 = 0)
       const int cell = qc[q * kQueueStride];
       float4 q4 = ldg4(sortedPos + j);
       float3 rel = make_float3(q4.x - pos.x, q4.y - pos.y, q4.z - pos.z);
@@ -227,7 +228,7 @@ __device__ __forceinline__ float3 neighbourForceGlobal(
       float3 rel = make_float3(q4.x - pos.x, q4.y - pos.y, q4.z - pos.z);
       float d2 = pairDist2(rel);
       float hi2 = kRadiusFromW ? rejectBound(ri + q4.w) : cdMonoHi2;
-      if (d2 < hi2 && j != i) {
+      if (d2 < hi2) {
         if (qn == kQueueLen) drain();
         qj[qn * kQueueStride] = j;
         qc[qn * kQueueStride] = (unsigned char)(cellA + (j >= m1) + (j >= m2));
@@ -306,7 +307,7 @@ __device__ __forceinline__ float3 neighbourForceGlobal(
         float3 rel = make_float3(q4.x - pos.x, q4.y - pos.y, q4.z - pos.z);
         float d2 = pairDist2(rel);
         float hi2 = kRadiusFromW ? rejectBound(ri + q4.w) : cdMonoHi2;
-        if (d2 < hi2 && j != i) {
+        if (d2 < hi2) {
           if (qn == kQueueLen) drain();
           qj[qn * kQueueStride] = j;
           qc[qn * kQueueStride] = (unsigned char)(row * 3 + x);
@@ -780,201 +781,6 @@ kCollideTiled(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
                                                 out, P);
 }
 
-// ---------------------------------------------------------------------------
-// Collide with one flattened candidate loop per thread (prefix cell table,
-// linear cell order).
-//
-// kCollideGlobal walks the nine neighbour rows one after the other, and the
-// lanes of a warp meet at the end of every row: a row costs the warp its
-// longest lane's range.  Here each thread first computes all nine ranges
-// (the table loads of all rows in flight together), the warp copies the
-// union of its lanes' ranges of every row that fits into shared memory, and
-// then each thread walks its nine ranges as one sequence in a single loop:
-// the warp costs its longest lane's whole neighbourhood, not the sum of nine
-// row maxima.  The candidate test, the near-partner queue and its drain are
-// kCollideGlobal's, so the sums are the same bits.  A particle whose rows
-// wrap in x, or with a row range above 1023 candidates, takes kCollideGlobal's
-// per-cell loop; crowded neighbourhoods are deferred to kCollideCrowd.
-constexpr int kFlatStage = 256;            // staged partner positions per warp
-constexpr unsigned kFlatLenMask = 1023u;   // row word: len | (o1 - a) << 10 | (o2 - a) << 20
-constexpr int kNotStaged = -2147483647 - 1;
-
-template <int kMode, bool kRadiusFromW, bool kCollider, bool kForceOut>
-__global__ void __launch_bounds__(128)
-kCollideFlat(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
-             const float4 *__restrict__ sortedVel, const unsigned *__restrict__ index,
-             CellRanges cells, unsigned n, KParams kp, CollideOut out, bool cull,
-             CrowdList crowd, unsigned *status) {
-  __shared__ uint2 sRow[9][128];              // per row and thread: start, row word
-  __shared__ float4 sStage[4][kFlatStage];    // per warp: the staged rows
-  __shared__ int sDelta[4][9];                // stage index - sorted index, or kNotStaged
-  __shared__ unsigned qj[kQueueLen * kQueueStride];
-  __shared__ unsigned char qc[kQueueLen * kQueueStride];
-  const SimParams &P = kp.p;
-  const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  const unsigned i = blockIdx.x * blockDim.x + tid;
-  const bool valid = i < n;
-  float4 p4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), v4 = p4;
-  if (valid) {
-    p4 = ldg4(sortedPos + i);
-    v4 = ldg4(sortedVel + i);
-  }
-  const float3 pos = make_float3(p4.x, p4.y, p4.z), vel = make_float3(v4.x, v4.y, v4.z);
-  const float ri = kRadiusFromW ? p4.w : P.particleRadius;
-  const int3 g = gridPos(pos.x, pos.y, pos.z, P);
-  bool lcull = cull;
-  if (valid && kRadiusFromW && !(ri <= P.particleRadius)) {
-    atomicOr(status, (unsigned)kStatusRadiusBound);
-    lcull = false;
-  }
-  const unsigned gxm = P.gridSize[0] - 1u;
-  const unsigned xm = (unsigned)g.x & gxm;
-  const bool merged = xm >= 1u && xm < gxm;
-  const bool inert = inertPos(pos);  // an inert particle's force is +0.0
-  bool flat = valid && merged && !inert;
-  const CellCull cc = makeCull(pos, g, ri + P.particleRadius, P);
-  const float cullR2 = lcull ? cc.r2 : __int_as_float(0x7f800000);
-  unsigned hood = 0u;
-#pragma unroll
-  for (int row = 0; row < 9; row++) {
-    const int z = row / 3 - 1, y = row % 3 - 1;
-    uint2 e = make_uint2(0u, 0u);
-    if (valid && merged) {
-      const unsigned h0 = gridHash(g.x - 1, g.y + y, g.z + z, P);
-      const unsigned q0 = __ldg(cells.off + h0), q1 = __ldg(cells.off + h0 + 1);
-      const unsigned q2 = __ldg(cells.off + h0 + 2), q3 = __ldg(cells.off + h0 + 3);
-      hood += q3 > q0 ? q3 - q0 : 0u;
-      const float rowD2 = CellCull::pick(z, cc.zl, cc.zh) + CellCull::pick(y, cc.yl, cc.yh);
-      if (rowD2 <= cullR2) {
-        const unsigned a = rowD2 + cc.xl <= cullR2 ? q0 : q1;
-        unsigned b = min(rowD2 + cc.xh <= cullR2 ? q3 : q2, n);
-        if (b < a) b = a;
-        const unsigned len = b - a;
-        if (len > kFlatLenMask) flat = false;  // too long for the row word
-        const unsigned d1 = q1 > a ? min(q1 - a, kFlatLenMask) : 0u;
-        const unsigned d2 = q2 > a ? min(q2 - a, kFlatLenMask) : 0u;
-        e = make_uint2(a, min(len, kFlatLenMask) | (d1 << 10) | (d2 << 20));
-      }
-    }
-    sRow[row][tid] = e;
-  }
-  bool mine = valid;
-  if (valid && !merged) hood = neighbourhoodCount<true>(g, cells, n, P);
-  if (valid && crowd.groups && hood > crowd.limit) {
-    unsigned a, b;
-    cellRange<true>(gridHash(g.x, g.y, g.z, P), cells, n, a, b);
-    if (i >= a && i < b) {  // deferred to kCollideCrowd with its cell's members
-      if (((i - a) & 31u) == 0u) {
-        const unsigned k = atomicAdd(crowd.count, 1u);
-        if (k < crowd.cap) crowd.groups[k] = make_uint2(i, min(32u, b - i));
-      }
-      mine = false;
-      flat = false;
-    }
-  }
-  if (!flat) {  // no rows to walk (and none to stage for this thread)
-#pragma unroll
-    for (int row = 0; row < 9; row++) sRow[row][tid] = make_uint2(0u, 0u);
-  }
-  __syncwarp();
-  // The union of the warp's ranges of each row, staged while they fit.
-  unsigned seg = 0u;
-#pragma unroll 1
-  for (int row = 0; row < 9; row++) {
-    const uint2 e = sRow[row][tid];
-    const unsigned len = e.y & kFlatLenMask;
-    const unsigned lo = __reduce_min_sync(0xffffffffu, len ? e.x : 0xffffffffu);
-    const unsigned hi = __reduce_max_sync(0xffffffffu, len ? e.x + len : 0u);
-    int delta = kNotStaged;
-    if (lo < hi && seg + (hi - lo) <= (unsigned)kFlatStage) {
-      for (unsigned t = lane; t < hi - lo; t += 32u) sStage[warp][seg + t] = ldg4(sortedPos + lo + t);
-      delta = (int)seg - (int)lo;
-      seg += hi - lo;
-    }
-    if (lane == 0) sDelta[warp][row] = delta;
-  }
-  __syncwarp();
-  float3 force = make_float3(0.0f, 0.0f, 0.0f);
-  if (flat) {
-    const float cdMono = ri + P.particleRadius;
-    const float cdMonoHi2 = rejectBound(cdMono);
-    unsigned *qjT = qj + tid;
-    unsigned char *qcT = qc + tid;
-    float3 cf = make_float3(0.0f, 0.0f, 0.0f);
-    int cfCell = -1;
-    int qn = 0;
-    auto drain = [&]() {
-      for (int q = 0; q < qn; ++q) {
-        const unsigned j = qjT[q * kQueueStride];
-        const int cell = qcT[q * kQueueStride];
-        const float4 q4 = ldg4(sortedPos + j);
-        const float3 rel = make_float3(q4.x - pos.x, q4.y - pos.y, q4.z - pos.z);
-        const float dist = sqrtf(pairDist2(rel));
-        const float cd = kRadiusFromW ? ri + q4.w : cdMono;
-        if (dist < cd) {
-          if (cell != cfCell) {
-            force.x = force.x + cf.x;
-            force.y = force.y + cf.y;
-            force.z = force.z + cf.z;
-            cf = make_float3(0.0f, 0.0f, 0.0f);
-            cfCell = cell;
-          }
-          const float4 w4 = ldg4(sortedVel + j);
-          const float3 f = contactTerm(rel, dist, cd, vel, make_float3(w4.x, w4.y, w4.z),
-                                       P.attraction, P);
-          cf.x = cf.x + f.x;
-          cf.y = cf.y + f.y;
-          cf.z = cf.z + f.z;
-        }
-      }
-      qn = 0;
-    };
-    // one loop over the nine ranges: row switches are the only divergence
-    int row = -1;
-    unsigned j = 0u, end = 0u, a = 0u, word = 0u;
-    int delta = kNotStaged;
-    for (;;) {
-      if (j == end) {
-        uint2 e = make_uint2(0u, 0u);
-        do {
-          if (++row == 9) break;
-          e = sRow[row][tid];
-        } while ((e.y & kFlatLenMask) == 0u);
-        if (row == 9) break;
-        a = e.x;
-        word = e.y;
-        j = a;
-        end = a + (word & kFlatLenMask);
-        delta = sDelta[warp][row];
-      }
-      const float4 q4 = delta != kNotStaged ? sStage[warp][(int)j + delta] : ldg4(sortedPos + j);
-      const float3 rel = make_float3(q4.x - pos.x, q4.y - pos.y, q4.z - pos.z);
-      const float d2 = pairDist2(rel);
-      const float hi2 = kRadiusFromW ? rejectBound(ri + q4.w) : cdMonoHi2;
-      if (d2 < hi2 && j != i) {
-        if (qn == kQueueLen) drain();
-        const unsigned o = j - a;
-        qjT[qn * kQueueStride] = j;
-        qcT[qn * kQueueStride] =
-            (unsigned char)(row * 3 + (o >= ((word >> 10) & kFlatLenMask)) +
-                            (o >= ((word >> 20) & kFlatLenMask)));
-        ++qn;
-      }
-      ++j;
-    }
-    drain();
-    force.x = force.x + cf.x;
-    force.y = force.y + cf.y;
-    force.z = force.z + cf.z;
-  } else if (mine && !inert) {  // rows that wrap in x, or a row above the word's length
-    force = neighbourForceGlobal<kRadiusFromW, true>(i, n, pos, vel, ri, g, lcull, sortedPos,
-                                                     sortedVel, cells, P, qj + tid, qc + tid);
-  }
-  if (mine)
-    finishParticle<kMode, kCollider, kForceOut>(i, n, pos, vel, p4, ri, force, index, newVel,
-                                                out, P);
-}
-
 bool g_crowdPath = true;  // fcdemSetCrowdPath
 unsigned g_crowdLimit = kCrowdLimit;  // fcdemSetCrowdLimit
 constexpr unsigned kCrowdCtasPerSm = 4;  // persistent grid: this many CTAs per SM
@@ -1006,7 +812,7 @@ CrowdList crowdList(unsigned n) {
 }
 
 template <int kMode, bool kRadiusFromW, bool kCollider, bool kForceOut, bool kPrefix>
-void launchT(bool tiled, bool warpPath, bool cull, unsigned n, float4 *newVel, const float4 *sp,
+void launchT(bool tiled, bool cull, unsigned n, float4 *newVel, const float4 *sp,
              const float4 *sv, const unsigned *index, const CellRanges &cells,
              const KParams &kp, const CollideOut &out) {
   unsigned blocks = (n + 127) / 128;
@@ -1014,19 +820,7 @@ void launchT(bool tiled, bool warpPath, bool cull, unsigned n, float4 *newVel, c
     kCollideTiled<kMode, kRadiusFromW, kCollider, kForceOut>
         <<<blocks, kTileThreads, 0, curStream()>>>(newVel, sp, sv, index, cells, n, kp, out,
                                                    ctx().dStatus);
-  else if (kPrefix && warpPath && kp.p.maxParticlesPerCell != kMortonTag) {
-    // the flattened-loop kernel; its crowded particles go to kCollideCrowd
-    const CrowdList crowd = crowdList(n);
-    kCollideFlat<kMode, kRadiusFromW, kCollider, kForceOut>
-        <<<blocks, 128, 0, curStream()>>>(newVel, sp, sv, index, cells, n, kp, out, cull, crowd,
-                                          ctx().dStatus);
-    if (crowd.groups && launchOk())
-      kCollideCrowd<kMode, kRadiusFromW, kCollider, kForceOut, kPrefix>
-          <<<numSms() * kCrowdCtasPerSm, kCrowdWarps * 32, 0, curStream()>>>(
-              newVel, sp, sv, index, cells, n, kp, out, cull, crowd, ctx().dStatus);
-    return;
-  }
-  if (!(tiled && !kPrefix)) {
+  else {
     const CrowdList crowd = crowdList(n);
     kCollideGlobal<kMode, kRadiusFromW, kCollider, kForceOut, kPrefix>
         <<<blocks, 128, 0, curStream()>>>(newVel, sp, sv, index, cells, n, kp, out, cull,
@@ -1106,7 +900,7 @@ kCollideBatch(const BatchScene *__restrict__ scenes, const unsigned *__restrict_
   }
 }
 
-int g_collidePath = -1;  // -1 auto, 0 global, 1 tiled, 2 warp (fcdemSetCollidePath)
+int g_collidePath = -1;  // -1 auto, 0 global, 1 tiled (fcdemSetCollidePath)
 bool g_cullCells = true;  // fcdemSetCellCulling
 
 }  // namespace
@@ -1121,8 +915,6 @@ void launchCollide(int mode, bool collider, float4 *newVel, const float4 *sp,
   // (its row windows assume the linear cell order)
   bool tiled = !prefix && g_collidePath == 1 && ((uintptr_t)sp & 15u) == 0 &&
                kp.p.maxParticlesPerCell != kMortonTag;
-  // the flattened-loop kernel reads the prefix table
-  const bool warpPath = prefix && g_collidePath == 2;
   // Culling is exact when every grid dimension is >= 3 and the largest
   // contact distance 2 * particleRadius fits in the smallest cell.
   const SimParams &P = kp.p;
@@ -1134,7 +926,7 @@ void launchCollide(int mode, bool collider, float4 *newVel, const float4 *sp,
   const bool fo = out.force != nullptr;
 #define FCDEM_COLLIDE_CASE(M, W, C, F, X)                                              \
   if (mode == M && w == W && collider == C && fo == F && prefix == X) {                \
-    launchT<M, W, C, F, X>(tiled, warpPath, cull, n, newVel, sp, sv, index, cells, kp, out); \
+    launchT<M, W, C, F, X>(tiled, cull, n, newVel, sp, sv, index, cells, kp, out);     \
     launchOk();                                                                        \
     return;                                                                            \
   }
@@ -1195,7 +987,7 @@ void launchCollideBatch(int mode, bool radiusFromW, const BatchScene *scenes,
 }  // namespace fcdem
 
 extern "C" void fcdemSetCollidePath(int path) {
-  fcdem::g_collidePath = (path >= 0 && path <= 2) ? path : -1;
+  fcdem::g_collidePath = (path == 0 || path == 1) ? path : -1;
 }
 
 extern "C" void fcdemSetCellCulling(int on) { fcdem::g_cullCells = on != 0; }

@@ -223,10 +223,8 @@ void fcdemUpdate(float *pos, float *vel, float *sortedPos, float *sortedVel,
                  uint *cellStart, uint *cellEnd, float deltaTime,
                  uint numParticles, uint numCells, uint steps);
 
-/* Collide kernel selection: -1 (default) automatic, 0 the per-thread
- * global-read kernel, 1 the shared-memory tiled kernel (split cell tables),
- * 2 the kernel with one flattened candidate loop per thread (prefix cell
- * table of fcdemUpdate and fcdemUM_update).  All give identical results. */
+/* Collide kernel selection: -1 (default) automatic, 0 the global-read
+ * kernel, 1 the shared-memory tiled kernel.  Both give identical results. */
 void fcdemSetCollidePath(int path);
 
 /* Test hook: the number of look-back rounds a tile of the radix sort

@@ -1,9 +1,8 @@
 """The collide kernels give bit-identical results: the per-thread kernel with
-global reads, the kernel with shared-memory tiles staged by bulk copies, the
-kernel with one flattened candidate loop per thread, and the kernel for
-crowded neighbourhoods, on
-scenes that exercise staged tiles, multi-row tiles, x-wrapping windows,
-crowded cells, inert particles and the polydisperse mode."""
+global reads, the kernel with shared-memory tiles staged by bulk copies, and
+the kernel for crowded neighbourhoods, on scenes that exercise staged tiles,
+multi-row tiles, x-wrapping windows, crowded cells, inert particles and the
+polydisperse mode."""
 import numpy as np
 import pytest
 
@@ -218,63 +217,3 @@ def test_crowd_limit_does_not_change_results(limit):
     for x, y in zip(a, b):
         np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
 
-
-def _run_path_update(sc, path, steps, um=False):
-    from fullc0ntact_gb300 import dem
-    dem.lib.fcdemSetCollidePath(path)
-    try:
-        ds = dem.UmScene(sc) if um else dem.DeviceScene(sc)
-        ds.update(steps)
-        dem.check("collide path %d" % path)
-        out = [ds.pos.cpu().numpy(), ds.vel.cpu().numpy(), ds.hash.cpu().numpy()]
-        if um:
-            out.append(ds.force.cpu().numpy())
-        return out
-    finally:
-        dem.lib.fcdemSetCollidePath(-1)
-
-
-@pytest.mark.parametrize("case", ["packed", "lattice", "wrap", "random_poly", "crowded",
-                                  "inert", "torus_um"])
-def test_flat_kernel_equals_per_thread(case):
-    """The collide with one flattened loop over the nine row ranges per
-    thread gives the per-row kernel's bits: five fused updates, on scenes
-    with x-wrapping rows (those particles take the per-cell loop), crowded
-    cells, inert particles, and the unified-memory step's evalForces."""
-    from fullc0ntact_gb300 import scenes
-    um = False
-    if case == "packed":
-        sc = scenes.packed_scene(200_000, grid=128)
-    elif case == "lattice":
-        sc = scenes.lattice_scene(16384)
-    elif case == "wrap":
-        sc = scenes.random_box(30000, grid=(32, 32, 32), radius=1.0 / 32.0, seed=8)
-    elif case == "random_poly":
-        sc = scenes.random_box(30000, grid=(64, 64, 64), radius=1.0 / 64.0, seed=9, poly=True)
-    elif case == "crowded":
-        sc = _crowded_scene("packed")
-    elif case == "inert":
-        sc = _inert_scene()
-    else:
-        sc, um = scenes.torus_fall_scene(100_000, z0=0.09), True
-    a = _run_path_update(sc, 0, 5, um)
-    b = _run_path_update(sc, 2, 5, um)
-    for x, y in zip(a, b):
-        np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
-
-
-def test_flat_kernel_long_rows_are_exact():
-    """With the crowd limit raised, crowded cells go through the flattened
-    kernel, and their row ranges grow past the 1023 candidates its row word
-    holds: those particles take the per-cell loop, and the results stay the
-    per-row kernel's bits."""
-    from fullc0ntact_gb300 import dem
-    sc = _crowded_scene("packed")
-    a = _run_path_update(sc, 0, 3)
-    dem.lib.fcdemSetCrowdLimit(1 << 20)
-    try:
-        b = _run_path_update(sc, 2, 3)
-    finally:
-        dem.lib.fcdemSetCrowdLimit(0)
-    for x, y in zip(a, b):
-        np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
