@@ -677,10 +677,17 @@ def cpu_baseline(sc: dict, steps: int) -> dict:
              nthreads=threads)
     dt = time.perf_counter() - t0
     n = pos.shape[0]
+    # one core: two more updates of the same scene on one thread
+    t0 = time.perf_counter()
+    O.update(P, pos, vel, sc["dt"], steps=2, radius_from_w=sc["radius_from_w"], nthreads=1)
+    dt1 = time.perf_counter() - t0
     return {"value": n * steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{steps} full updates of the {n}-sphere scene "
                       f"(collide on {threads} threads, other stages on 1)",
-            "seconds": dt}
+            "seconds": dt,
+            "single_core": {"value": n * 2 / dt1, "unit": UNIT, "cores": 1,
+                            "sample": f"the next 2 updates of the same scene on one thread",
+                            "seconds": dt1}}
 
 
 def dist_env():

@@ -195,7 +195,6 @@ __device__ __forceinline__ float3 neighbourForceGlobal(
   auto drain = [&]() {
     for (int q = 0; q < qn; ++q) {
       const unsigned j = qj[q * kQueueStride];
-      if (j == i) continue;  // the scans queue the particle itself (d2 = 0)
       const int cell = qc[q * kQueueStride];
       float4 q4 = ldg4(sortedPos + j);
       float3 rel = make_float3(q4.x - pos.x, q4.y - pos.y, q4.z - pos.z);
@@ -228,7 +227,7 @@ __device__ __forceinline__ float3 neighbourForceGlobal(
       float3 rel = make_float3(q4.x - pos.x, q4.y - pos.y, q4.z - pos.z);
       float d2 = pairDist2(rel);
       float hi2 = kRadiusFromW ? rejectBound(ri + q4.w) : cdMonoHi2;
-      if (d2 < hi2) {
+      if (d2 < hi2 && j != i) {
         if (qn == kQueueLen) drain();
         qj[qn * kQueueStride] = j;
         qc[qn * kQueueStride] = (unsigned char)(cellA + (j >= m1) + (j >= m2));
@@ -307,7 +306,7 @@ __device__ __forceinline__ float3 neighbourForceGlobal(
         float3 rel = make_float3(q4.x - pos.x, q4.y - pos.y, q4.z - pos.z);
         float d2 = pairDist2(rel);
         float hi2 = kRadiusFromW ? rejectBound(ri + q4.w) : cdMonoHi2;
-        if (d2 < hi2) {
+        if (d2 < hi2 && j != i) {
           if (qn == kQueueLen) drain();
           qj[qn * kQueueStride] = j;
           qc[qn * kQueueStride] = (unsigned char)(row * 3 + x);
