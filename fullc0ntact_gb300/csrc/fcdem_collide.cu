@@ -181,7 +181,7 @@ __device__ __forceinline__ float3 neighbourForceGlobal(
     unsigned i, unsigned n, float3 pos, float3 vel, float ri, int3 g, bool cull,
     const float4 *__restrict__ sortedPos, const float4 *__restrict__ sortedVel,
     const CellRanges &cells, const SimParams &P, unsigned *qj, unsigned char *qc,
-    float4 *stage = nullptr) {
+    float4 *stage = nullptr, unsigned live = 0u) {
   const float cdMono = ri + P.particleRadius;
   const float cdMonoHi2 = rejectBound(cdMono);
   // largest contact distance: r_i + particleRadius (in the radius-from-w
@@ -263,16 +263,20 @@ __device__ __forceinline__ float3 neighbourForceGlobal(
         // The lanes of a warp are consecutive sorted particles, mostly in
         // one grid row: their ranges of this neighbour row overlap.  The
         // warp copies the union into shared memory with coalesced loads and
-        // every lane scans its own range from there.
-        const unsigned am = __activemask();
-        const unsigned lo = __reduce_min_sync(am, a < b ? a : 0xffffffffu);
-        const unsigned hi = __reduce_max_sync(am, a < b ? b : 0u);
+        // every lane scans its own range from there.  `live` is every lane
+        // of the warp that calls this function (fixed by a ballot before
+        // the call): all of them take part in each row's reductions, so a
+        // row's copy is never written while a group of lanes that fell
+        // behind (in a drain, or in a row scanned from global memory) still
+        // reads the previous one.
+        const unsigned lo = __reduce_min_sync(live, a < b ? a : 0xffffffffu);
+        const unsigned hi = __reduce_max_sync(live, a < b ? b : 0u);
         if (lo < hi && hi - lo <= (unsigned)kStageLen) {
-          const unsigned rank = __popc(am & ((1u << lane) - 1u)), lanes = __popc(am);
+          const unsigned rank = __popc(live & ((1u << lane) - 1u)), lanes = __popc(live);
           for (unsigned t = rank; t < hi - lo; t += lanes) stage[t] = ldg4(sortedPos + lo + t);
-          __syncwarp(am);
+          __syncwarp(live);
           scanRange(a, b, row * 3, o1, o2, [&](unsigned j) { return stage[j - lo]; });
-          __syncwarp(am);  // the copy is reused by the next row
+          __syncwarp(live);  // the copy is reused by the next row
         } else if (merged) {
           scanRange(a, b, row * 3, o1, o2, loadGlobal);
         }
@@ -405,15 +409,17 @@ kCollideGlobal(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos
   __shared__ unsigned char qc[kQueueLen * kQueueStride];
   __shared__ float4 sStage[4][kStageLen];
   const SimParams &P = kp.p;
-  unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  float4 p4 = ldg4(sortedPos + i);
-  float4 v4 = ldg4(sortedVel + i);
-  float3 pos = make_float3(p4.x, p4.y, p4.z), vel = make_float3(v4.x, v4.y, v4.z);
-  float ri = kRadiusFromW ? p4.w : P.particleRadius;
-  int3 g = gridPos(pos.x, pos.y, pos.z, P);
-  if (crowd.groups &&
-      neighbourhoodCount<kPrefix>(g, cells, n, P) > crowd.limit) {
+  const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  // every lane of the warp reaches the ballot below (the block is whole
+  // warps); lanes past n load nothing
+  const bool active = i < n;
+  const float4 p4 = active ? ldg4(sortedPos + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  const float4 v4 = active ? ldg4(sortedVel + i) : p4;
+  const float3 pos = make_float3(p4.x, p4.y, p4.z), vel = make_float3(v4.x, v4.y, v4.z);
+  const float ri = kRadiusFromW ? p4.w : P.particleRadius;
+  const int3 g = gridPos(pos.x, pos.y, pos.z, P);
+  bool deferred = false;
+  if (active && crowd.groups && neighbourhoodCount<kPrefix>(g, cells, n, P) > crowd.limit) {
     unsigned a, b;
     cellRange<kPrefix>(gridHash(g.x, g.y, g.z, P), cells, n, a, b);
     if (i >= a && i < b) {  // deferred to kCollideCrowd
@@ -421,18 +427,22 @@ kCollideGlobal(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos
         const unsigned k = atomicAdd(crowd.count, 1u);
         if (k < crowd.cap) crowd.groups[k] = make_uint2(i, min(32u, b - i));
       }
-      return;
+      deferred = true;
     }
   }
-  if (kRadiusFromW && !(ri <= P.particleRadius)) {  // the culling bound is broken
-    atomicOr(status, (unsigned)kStatusRadiusBound);
+  if (active && !deferred && kRadiusFromW && !(ri <= P.particleRadius)) {
+    atomicOr(status, (unsigned)kStatusRadiusBound);  // the culling bound is broken
     cull = false;
   }
+  // an inert particle's force is +0.0 (inertPos): it scans nothing
+  const bool scan = active && !deferred && !inertPos(pos);
+  const unsigned live = __ballot_sync(0xffffffffu, scan);
+  if (!active || deferred) return;
   float3 force = make_float3(0.0f, 0.0f, 0.0f);
-  if (!inertPos(pos))  // an inert particle's force is +0.0 (inertPos)
+  if (scan)
     force = neighbourForceGlobal<kRadiusFromW, kPrefix>(
         i, n, pos, vel, ri, g, cull, sortedPos, sortedVel, cells, P, qj + threadIdx.x,
-        qc + threadIdx.x, kPrefix ? sStage[threadIdx.x >> 5] : nullptr);
+        qc + threadIdx.x, kPrefix ? sStage[threadIdx.x >> 5] : nullptr, live);
   finishParticle<kMode, kCollider, kForceOut>(i, n, pos, vel, p4, ri, force, index, newVel,
                                               out, P);
 }

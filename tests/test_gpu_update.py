@@ -192,3 +192,30 @@ def test_counting_pipeline_many_tiles():
     np.testing.assert_array_equal(sa, sb)
     occ = sa != 0xFFFFFFFF
     np.testing.assert_array_equal(dem.u32(a.cell_end)[occ], dem.u32(b.cell_end)[occ])
+
+
+@pytest.mark.parametrize("crowd", [1, 0])
+def test_staged_rows_with_many_contacts_equal_staged_calls(crowd):
+    """Dense scenes where the lanes of a warp fall out of step inside a
+    neighbour row: about 60 contacts per sphere (several queue drains per
+    row), warps that mix spheres of edge columns (rows walked cell by cell)
+    with interior ones (rows copied to shared memory), and -- with the
+    crowded-neighbourhood kernel switched off -- collapsed cells whose rows
+    are too long to copy.  The fused update, whose collide copies each row
+    once per warp, against the reference-named stages, whose collide reads
+    every partner from global memory: the same bits over four steps."""
+    from fullc0ntact_gb300 import dem, scenes
+    from test_gpu_collide_paths import _crowded_scene
+    dem.lib.fcdemSetCrowdPath(crowd)
+    try:
+        for sc in (scenes.random_box(60000, grid=(16, 16, 16), radius=1.0 / 16.0, seed=14),
+                   _crowded_scene("packed")):
+            a, b = dem.DeviceScene(sc), dem.DeviceScene(sc)
+            for _ in range(4):
+                a.stages()
+            b.update(4)
+            dem.check("update")
+            for x, y in zip(_state(a), _state(b)):
+                np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
+    finally:
+        dem.lib.fcdemSetCrowdPath(1)
