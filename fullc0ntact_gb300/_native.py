@@ -59,6 +59,8 @@ _SIGS = {
     "fcdemAutotuneSort": (C.c_int, [C.c_uint, C.c_uint, C.POINTER(C.c_float)]),
     "fcdemSetSortConfig": (C.c_int, [C.c_uint, C.c_int]),
     "fcdemSetSortWaitLimit": (None, [C.c_int]),
+    "fcdemWriteVtkParticles": (C.c_int, [C.c_char_p, vp, vp, u32, C.c_float, C.c_int]),
+    "fcdemWriteGPUParticleFile": (C.c_int, [vp, u32, C.c_char_p]),
 }
 
 for _name, (_res, _args) in _SIGS.items():

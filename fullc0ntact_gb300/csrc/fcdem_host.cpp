@@ -13,13 +13,20 @@
 
 using fcdem_rng::uniformF;
 
-extern "C" int fcdemWriteVtkParticles(const char *path, const float *pos4, const float *vel4,
-                                      uint n, float radius, int radiusFromW) {
+namespace {
+
+// The legacy ASCII VTK particle file of CVtkWriter::WriteGPUParticleFile
+// (inshape3dcore/postprocessing/vtkwriter.cpp:3399-3452): header, the points,
+// a "radius" scalar (radiusOf(i)), a "myid" scalar, and -- when vel4 is not
+// NULL -- a "velocity" vector.
+template <class RadiusOf>
+int writeParticleVtk(const char *path, const char *generator, const float *pos4,
+                     const float *vel4, uint n, RadiusOf radiusOf) {
   if (!path || (n && !pos4)) return FCDEM_ERR_INVALID_VALUE;
   FILE *f = std::fopen(path, "w");
   if (!f) return FCDEM_ERR_INVALID_VALUE;
   std::fprintf(f, "# vtk DataFile Version 2.0\n");
-  std::fprintf(f, "Generated by fcdem-gb300\n");
+  std::fprintf(f, "Generated by %s\n", generator);
   std::fprintf(f, "ASCII\n");
   std::fprintf(f, "DATASET UNSTRUCTURED_GRID\n");
   std::fprintf(f, "POINTS %u double\n", n);
@@ -29,8 +36,7 @@ extern "C" int fcdemWriteVtkParticles(const char *path, const float *pos4, const
   std::fprintf(f, "POINT_DATA %u\n", n);
   std::fprintf(f, "SCALARS radius double 1\n");
   std::fprintf(f, "LOOKUP_TABLE default\n");
-  for (uint i = 0; i < n; ++i)
-    std::fprintf(f, "%f \n", radiusFromW ? pos4[4 * (size_t)i + 3] : radius);
+  for (uint i = 0; i < n; ++i) std::fprintf(f, "%f \n", radiusOf(i));
   std::fprintf(f, "SCALARS myid double 1\n");
   std::fprintf(f, "LOOKUP_TABLE default\n");
   for (uint i = 0; i < n; ++i) std::fprintf(f, "%f \n", (float)i);
@@ -43,6 +49,22 @@ extern "C" int fcdemWriteVtkParticles(const char *path, const float *pos4, const
   int bad = std::ferror(f);
   std::fclose(f);
   return bad ? FCDEM_ERR_INVALID_VALUE : FCDEM_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" int fcdemWriteVtkParticles(const char *path, const float *pos4, const float *vel4,
+                                      uint n, float radius, int radiusFromW) {
+  return writeParticleVtk(path, "fcdem-gb300", pos4, vel4, n, [&](uint i) {
+    return radiusFromW ? pos4[4 * (size_t)i + 3] : radius;
+  });
+}
+
+extern "C" int fcdemWriteGPUParticleFile(const float *pos4, uint n, const char *path) {
+  // the reference's own bytes: its generator line and a radius of 1/64 for
+  // every particle, no velocity
+  return writeParticleVtk(path, "InShape 2.x", pos4, nullptr, n,
+                          [](uint) { return 1.0f / 64.0f; });
 }
 
 // ---------------------------------------------------------------------------

@@ -466,6 +466,15 @@ void fcdemBatchUpdate(fcdemBatch *batch, float *pos, float *vel, float deltaTime
 int fcdemWriteVtkParticles(const char *path, const float *pos4, const float *vel4,
                            uint n, float radius, int radiusFromW);
 
+/* CVtkWriter::WriteGPUParticleFile(pPos, strFileName)
+ * (inshape3dcore/postprocessing/vtkwriter.cpp:3399-3452) byte for byte: the
+ * reference's header lines, the n positions of pos4 (4 floats each, as the
+ * reference's pPos vector), a radius of 1/64 for every particle and the
+ * "myid" scalar.  Where the reference prints a message and exits the
+ * process when the file cannot be opened, this returns
+ * FCDEM_ERR_INVALID_VALUE. */
+int fcdemWriteGPUParticleFile(const float *pos4, uint n, const char *path);
+
 /* ---------------------------------------------------------------------- */
 /* Scene generators (host memory, 4 floats per particle).  Deterministic for
  * a given seed on every platform. */

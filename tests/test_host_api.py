@@ -35,6 +35,29 @@ def test_vtk_writer_format(tmp_path):
                                       0.1, 0) != 0
 
 
+def test_gpu_particle_file_is_the_reference_format(tmp_path):
+    """fcdemWriteGPUParticleFile writes the bytes of the reference's
+    CVtkWriter::WriteGPUParticleFile (vtkwriter.cpp:3399-3452): its four
+    header lines, "POINTS n double", each point as three %f fields and a
+    trailing space, POINT_DATA, the radius 1/64 for every particle and the
+    particle numbers as the "myid" scalar."""
+    from fullc0ntact_gb300 import _native
+    lib = _native.lib
+    rng = np.random.default_rng(5)
+    pos = rng.uniform(-1.0, 1.0, (37, 4)).astype(np.float32)
+    path = str(tmp_path / "gpu.vtk")
+    assert lib.fcdemWriteGPUParticleFile(pos.ctypes.data, 37, path.encode()) == 0
+    want = ["# vtk DataFile Version 2.0", "Generated by InShape 2.x", "ASCII",
+            "DATASET UNSTRUCTURED_GRID", "POINTS 37 double"]
+    want += ["%f %f %f " % tuple(float(v) for v in p[:3]) for p in pos]
+    want += ["POINT_DATA 37", "SCALARS radius double 1", "LOOKUP_TABLE default"]
+    want += ["%f " % float(np.float32(1.0 / 64.0))] * 37
+    want += ["SCALARS myid double 1", "LOOKUP_TABLE default"]
+    want += ["%f " % float(i) for i in range(37)]
+    assert open(path, "rb").read() == ("\n".join(want) + "\n").encode()
+    assert lib.fcdemWriteGPUParticleFile(pos.ctypes.data, 37, b"/nonexistent/dir/p.vtk") != 0
+
+
 def test_particledem_header_compiles_and_links():
     from fullc0ntact_gb300 import _native
     src = r'''
