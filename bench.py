@@ -799,6 +799,15 @@ def run_ours(args):
     if args.advance > 0:
         ds.update(args.advance)
         dem.check("advance")
+    # project autotuner: collide's crowd limit, crowded-kernel grid and row
+    # staging, timed on one step from the job's start state (setup, untimed;
+    # every configuration gives the same bits)
+    collide_cfg, collide_tuned_ms = ds.autotune_collide()
+    lim, ctas, stage = C.c_uint(), C.c_uint(), C.c_int()
+    lib.fcdemGetCollideConfig(collide_cfg, C.byref(lim), C.byref(ctas), C.byref(stage))
+    collide_cfg_desc = {"index": collide_cfg, "crowd_limit": lim.value,
+                        "crowd_ctas_per_sm": ctas.value, "row_staging": bool(stage.value),
+                        "tuned_step_ms": collide_tuned_ms}
     pos0, vel0 = ds.pos.clone(), ds.vel.clone()
 
     def reset():
@@ -948,7 +957,8 @@ def run_ours(args):
             "data": "synthetic (seeded packing)",
             "config": job_config(args, n),
             "job": {"occupied_cells": occupied, "step": "fcdemUpdate (fused update)",
-                    "sort_config": sort_cfg, "cell_order": args.cell_order},
+                    "sort_config": sort_cfg, "collide_config": collide_cfg_desc,
+                    "cell_order": args.cell_order},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
                     "d2h_bytes_per_step": 2 * nbytes, "steps": e2e_steps,
                     "path": "copyArrayToDevice x2, fcdemUpdate, copyArrayFromDevice x2"},

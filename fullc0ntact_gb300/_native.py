@@ -59,6 +59,10 @@ _SIGS = {
     "fcdemAutotuneSort": (C.c_int, [C.c_uint, C.c_uint, C.POINTER(C.c_float)]),
     "fcdemSetSortConfig": (C.c_int, [C.c_uint, C.c_int]),
     "fcdemSetSortWaitLimit": (None, [C.c_int]),
+    "fcdemAutotuneCollide": (C.c_int, [vp] * 8 + [C.c_float, u32, u32, C.POINTER(C.c_float)]),
+    "fcdemSetCollideConfig": (C.c_int, [C.c_int]),
+    "fcdemGetCollideConfig": (C.c_int, [C.c_int, C.POINTER(C.c_uint), C.POINTER(C.c_uint),
+                                        C.POINTER(C.c_int)]),
     "fcdemWriteVtkParticles": (C.c_int, [C.c_char_p, vp, vp, u32, C.c_float, C.c_int]),
     "fcdemWriteGPUParticleFile": (C.c_int, [vp, u32, C.c_char_p]),
 }

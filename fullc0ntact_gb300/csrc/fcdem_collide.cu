@@ -404,7 +404,7 @@ __global__ void __launch_bounds__(128)
 kCollideGlobal(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
                const float4 *__restrict__ sortedVel, const unsigned *__restrict__ index,
                CellRanges cells, unsigned n, KParams kp, CollideOut out, bool cull,
-               CrowdList crowd, unsigned *status) {
+               CrowdList crowd, unsigned *status, bool stageRows) {
   __shared__ unsigned qj[kQueueLen * kQueueStride];
   __shared__ unsigned char qc[kQueueLen * kQueueStride];
   __shared__ float4 sStage[4][kStageLen];
@@ -442,7 +442,7 @@ kCollideGlobal(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos
   if (scan)
     force = neighbourForceGlobal<kRadiusFromW, kPrefix>(
         i, n, pos, vel, ri, g, cull, sortedPos, sortedVel, cells, P, qj + threadIdx.x,
-        qc + threadIdx.x, kPrefix ? sStage[threadIdx.x >> 5] : nullptr, live);
+        qc + threadIdx.x, kPrefix && stageRows ? sStage[threadIdx.x >> 5] : nullptr, live);
   finishParticle<kMode, kCollider, kForceOut>(i, n, pos, vel, p4, ri, force, index, newVel,
                                               out, P);
 }
@@ -792,7 +792,30 @@ kCollideTiled(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos,
 
 bool g_crowdPath = true;  // fcdemSetCrowdPath
 unsigned g_crowdLimit = kCrowdLimit;  // fcdemSetCrowdLimit
-constexpr unsigned kCrowdCtasPerSm = 4;  // persistent grid: this many CTAs per SM
+constexpr unsigned kCrowdCtasPerSmDefault = 4;
+unsigned g_crowdCtasPerSm = kCrowdCtasPerSmDefault;  // persistent grid: CTAs per SM
+bool g_stageRows = true;  // kCollideGlobal copies short row unions to shared memory
+
+// The collide configurations fcdemAutotuneCollide chooses from: crowd
+// limit x crowded-kernel CTAs per SM x row staging.  Results are identical
+// for every one; configuration kDefaultCollideConfig is the built-in one.
+struct CollideConfig {
+  unsigned crowdLimit, ctasPerSm;
+  bool stageRows;
+};
+constexpr unsigned kTuneLimits[] = {256u, 384u, 512u, 768u, 1024u};
+constexpr unsigned kTuneCtas[] = {2u, 4u, 8u};
+constexpr int kNumCollideConfigs = 5 * 3 * 2;
+constexpr int kDefaultCollideConfig = (2 * 3 + 1) * 2;  // 512, 4, staged
+CollideConfig collideConfig(int k) {
+  return CollideConfig{kTuneLimits[k / 6], kTuneCtas[(k / 2) % 3], (k % 2) == 0};
+}
+void applyCollideConfig(int k) {
+  const CollideConfig c = collideConfig(k);
+  g_crowdLimit = c.crowdLimit;
+  g_crowdCtasPerSm = c.ctasPerSm;
+  g_stageRows = c.stageRows;
+}
 
 // The group list for n particles (grown on demand; at most one group per
 // particle), its counters cleared on the current stream.  groups == nullptr
@@ -833,12 +856,11 @@ void launchT(bool tiled, bool cull, unsigned n, float4 *newVel, const float4 *sp
     const CrowdList crowd = crowdList(n);
     kCollideGlobal<kMode, kRadiusFromW, kCollider, kForceOut, kPrefix>
         <<<blocks, 128, 0, curStream()>>>(newVel, sp, sv, index, cells, n, kp, out, cull,
-                                          crowd, ctx().dStatus);
+                                          crowd, ctx().dStatus, g_stageRows);
     if (crowd.groups && launchOk())
       kCollideCrowd<kMode, kRadiusFromW, kCollider, kForceOut, kPrefix>
-          <<<numSms() * kCrowdCtasPerSm, kCrowdWarps * 32, 0, curStream()>>>(newVel, sp, sv, index, cells, n,
-                                                             kp, out, cull, crowd,
-                                                             ctx().dStatus);
+          <<<numSms() * g_crowdCtasPerSm, kCrowdWarps * 32, 0, curStream()>>>(
+              newVel, sp, sv, index, cells, n, kp, out, cull, crowd, ctx().dStatus);
   }
 }
 
@@ -1005,4 +1027,94 @@ extern "C" void fcdemSetCrowdPath(int on) { fcdem::g_crowdPath = on != 0; }
 
 extern "C" void fcdemSetCrowdLimit(unsigned limit) {
   fcdem::g_crowdLimit = limit ? limit : fcdem::kCrowdLimit;
+}
+
+extern "C" int fcdemSetCollideConfig(int config) {
+  using namespace fcdem;
+  applyCollideConfig(config >= 0 && config < kNumCollideConfigs ? config
+                                                                  : kDefaultCollideConfig);
+  return kNumCollideConfigs;
+}
+
+extern "C" int fcdemGetCollideConfig(int config, unsigned *crowdLimit, unsigned *ctasPerSm,
+                                     int *stageRows) {
+  using namespace fcdem;
+  if (config < 0 || config >= kNumCollideConfigs) {
+    setError(FCDEM_ERR_INVALID_VALUE);
+    return -1;
+  }
+  const CollideConfig c = collideConfig(config);
+  if (crowdLimit) *crowdLimit = c.crowdLimit;
+  if (ctasPerSm) *ctasPerSm = c.ctasPerSm;
+  if (stageRows) *stageRows = c.stageRows ? 1 : 0;
+  return 0;
+}
+
+extern "C" int fcdemAutotuneCollide(float *pos, float *vel, float *sortedPos, float *sortedVel,
+                                    unsigned *gridParticleHash, unsigned *gridParticleIndex,
+                                    unsigned *cellStart, unsigned *cellEnd, float deltaTime,
+                                    unsigned numParticles, unsigned numCells, float *bestMs) {
+  using namespace fcdem;
+  const unsigned n = numParticles;
+  if (n == 0 || !pos || !vel) {
+    setError(FCDEM_ERR_INVALID_VALUE);
+    return -1;
+  }
+  cudaStream_t st = curStream();
+  const size_t bytes = (size_t)n * 16;
+  float *save = nullptr;
+  if (cudaMalloc(&save, 2 * bytes) != cudaSuccess) {
+    cudaGetLastError();
+    setError(FCDEM_ERR_ALLOC);
+    return -1;
+  }
+  // the caller's state, put back before every trial and at the end
+  cudaMemcpyAsync(save, pos, bytes, cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(save + 4 * (size_t)n, vel, bytes, cudaMemcpyDeviceToDevice, st);
+  auto restore = [&]() {
+    cudaMemcpyAsync(pos, save, bytes, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(vel, save + 4 * (size_t)n, bytes, cudaMemcpyDeviceToDevice, st);
+  };
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int best = kDefaultCollideConfig;
+  float bestT = 3.4e38f, defaultT = 3.4e38f;
+  bool ok = true;
+  for (int k = 0; k < kNumCollideConfigs && ok; ++k) {
+    applyCollideConfig(k);
+    float tot = 0.0f;
+    for (int rep = 0; rep < 3 && ok; ++rep) {
+      restore();
+      cudaEventRecord(e0, st);
+      fcdemUpdate(pos, vel, sortedPos, sortedVel, gridParticleHash, gridParticleIndex,
+                  cellStart, cellEnd, deltaTime, n, numCells, 1);
+      cudaEventRecord(e1, st);
+      ok = cudaOk(cudaEventSynchronize(e1));
+      float t = 0.0f;
+      cudaEventElapsedTime(&t, e0, e1);
+      if (rep > 0) tot += t;  // the first run warms up
+    }
+    if (ok && k == kDefaultCollideConfig) defaultT = tot;
+    if (ok && tot < bestT) {
+      bestT = tot;
+      best = k;
+    }
+  }
+  // Where the scene has few crowded neighbourhoods the configurations differ
+  // by noise; the default is kept unless another one is 2% faster (a state
+  // tuned early in a job may crowd later, where the default's limit is best).
+  if (!(bestT < 0.98f * defaultT)) {
+    best = kDefaultCollideConfig;
+    bestT = defaultT;
+  }
+  applyCollideConfig(best);
+  restore();
+  cudaOk(cudaStreamSynchronize(st));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(save);
+  if (!ok) return -1;
+  if (bestMs) *bestMs = bestT / 2.0f;
+  return best;
 }

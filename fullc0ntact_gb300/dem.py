@@ -123,6 +123,20 @@ class DeviceScene:
                self.index, self.cell_start, self.cell_end, dt, self.n, self.num_cells,
                steps)
 
+    def autotune_collide(self, dt: float | None = None) -> tuple[int, float]:
+        """fcdemAutotuneCollide from this scene's state: the index of the
+        fastest collide configuration (kept for later updates) and its step
+        time in ms.  pos and vel are left as they were."""
+        dt = self.dt if dt is None else dt
+        self.activate()
+        ms = C.c_float()
+        k = lib.fcdemAutotuneCollide(_p(self.pos), _p(self.vel), _p(self.sorted_pos),
+                                     _p(self.sorted_vel), _p(self.hash), _p(self.index),
+                                     _p(self.cell_start), _p(self.cell_end), dt, self.n,
+                                     self.num_cells, C.byref(ms))
+        check("fcdemAutotuneCollide")
+        return int(k), float(ms.value)
+
 
 def u32(t: torch.Tensor) -> np.ndarray:
     """int32 device tensor -> uint32 host array (same bits)."""

@@ -244,6 +244,26 @@ void fcdemSetSortWaitLimit(int rounds);
 int fcdemAutotuneSort(unsigned numParticles, unsigned numCells, float *bestMs);
 int fcdemSetSortConfig(unsigned numParticles, int config);
 
+/* Collide tuning.  A collide configuration is a crowd limit (256, 384, 512,
+ * 768 or 1024 neighbourhood members; fcdemSetCrowdLimit), the CTAs per SM of
+ * the crowded-neighbourhood kernel's persistent grid (2, 4 or 8) and whether
+ * the per-particle kernel copies short neighbour rows to shared memory;
+ * results are identical for every one.  fcdemAutotuneCollide times one
+ * fcdemUpdate step from the caller's state (the arguments of fcdemUpdate)
+ * under each configuration, keeps the fastest -- the default unless another
+ * is at least 2% faster -- and returns its index (-1 on error); *bestMs
+ * receives its step time.  pos and vel are put back as they
+ * were (a temporary device copy); the work arrays hold one step's values.
+ * fcdemSetCollideConfig forces one (-1: the default, 512 / 4 / staged) and
+ * returns the number of configurations; fcdemGetCollideConfig describes
+ * configuration `config` (returns 0, or -1 for an index out of range). */
+int fcdemAutotuneCollide(float *pos, float *vel, float *sortedPos, float *sortedVel,
+                         uint *gridParticleHash, uint *gridParticleIndex, uint *cellStart,
+                         uint *cellEnd, float deltaTime, uint numParticles, uint numCells,
+                         float *bestMs);
+int fcdemSetCollideConfig(int config);
+int fcdemGetCollideConfig(int config, uint *crowdLimit, uint *ctasPerSm, int *stageRows);
+
 /* Number of kernels this library has launched in this process. */
 unsigned long long fcdemGetLaunchCount(void);
 

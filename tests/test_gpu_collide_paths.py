@@ -217,3 +217,48 @@ def test_crowd_limit_does_not_change_results(limit):
     for x, y in zip(a, b):
         np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
 
+
+
+def test_collide_configurations_give_identical_results():
+    """Three fused updates of the packed scene with collapsed cells under
+    collide configurations that differ in crowd limit, persistent-grid width
+    and row staging: the same bits as the default configuration."""
+    from fullc0ntact_gb300 import dem
+    sc = _crowded_scene("packed")
+    dem.lib.fcdemSetCollideConfig(-1)
+    ref = _run_crowd(sc, True, 3)
+    try:
+        for k in (0, 1, 7, 15, 22, 29):
+            dem.lib.fcdemSetCollideConfig(k)
+            got = _run_crowd(sc, True, 3)
+            for x, y in zip(ref, got):
+                np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
+    finally:
+        dem.lib.fcdemSetCollideConfig(-1)
+
+
+def test_collide_autotuner_keeps_the_state_and_the_results():
+    """fcdemAutotuneCollide on the packed scene with collapsed cells: it returns
+    a configuration index and a step time, puts pos and vel back as they were,
+    and the next update under the chosen configuration gives the bits of the
+    default one."""
+    import torch
+    from fullc0ntact_gb300 import dem
+    sc = _crowded_scene("packed")
+    ds = dem.DeviceScene(sc)
+    pos0, vel0 = ds.pos.clone(), ds.vel.clone()
+    k, ms = ds.autotune_collide()
+    try:
+        assert 0 <= k < 30 and ms > 0.0
+        assert torch.equal(ds.pos.view(torch.int32), pos0.view(torch.int32))
+        assert torch.equal(ds.vel.view(torch.int32), vel0.view(torch.int32))
+        ds.update(2)
+        dem.check("update after autotune")
+        tuned = (ds.pos.cpu().numpy(), ds.vel.cpu().numpy())
+    finally:
+        dem.lib.fcdemSetCollideConfig(-1)
+    ds2 = dem.DeviceScene(sc)
+    ds2.update(2)
+    dem.check("update, default configuration")
+    for x, y in zip(tuned, (ds2.pos.cpu().numpy(), ds2.vel.cpu().numpy())):
+        np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))

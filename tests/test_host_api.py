@@ -104,3 +104,21 @@ def test_scene_generators_are_deterministic():
     np.testing.assert_array_equal(a["pos"], b["pos"])
     c, d = scenes.packed_scene(3000, grid=32), scenes.packed_scene(3000, grid=32)
     np.testing.assert_array_equal(c["pos"], d["pos"])
+
+
+def test_collide_configuration_table():
+    """The collide configurations the autotuner chooses from: 5 crowd limits x
+    3 persistent-grid widths x row staging on/off, the default (512, 4 CTAs
+    per SM, staged) among them.  Reading the table needs no GPU."""
+    from fullc0ntact_gb300 import _native
+    lib = _native.lib
+    count = lib.fcdemSetCollideConfig(-1)
+    assert count == 30
+    seen = set()
+    for k in range(count):
+        lim, ctas, stage = C.c_uint(), C.c_uint(), C.c_int()
+        assert lib.fcdemGetCollideConfig(k, C.byref(lim), C.byref(ctas), C.byref(stage)) == 0
+        seen.add((lim.value, ctas.value, stage.value))
+    assert len(seen) == 30 and (512, 4, 1) in seen
+    assert {s[0] for s in seen} == {256, 384, 512, 768, 1024}
+    assert {s[1] for s in seen} == {2, 4, 8}
