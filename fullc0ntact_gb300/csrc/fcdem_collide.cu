@@ -221,7 +221,12 @@ __device__ __forceinline__ float3 neighbourForceGlobal(
   // queue a near partner j of neighbour cell `cell` (0..26); load(j) gives
   // the position of sorted particle j (global or the warp's staged copy)
   auto scanRange = [&](unsigned a, unsigned b, int cellA, unsigned m1, unsigned m2, auto load) {
-    // cells cellA, cellA+1, cellA+2 hold [a, m1), [m1, m2), [m2, b)
+    // cells cellA, cellA+1, cellA+2 hold [a, m1), [m1, m2), [m2, b).
+    // Two candidates per iteration: their dependent test chains overlap
+    // (0.778 against 0.810 ms of collide per 4.2M-sphere step early in the
+    // packed job; unrolled by 4, or with more registers by a minimum-blocks
+    // launch bound, it is slower).
+#pragma unroll 2
     for (unsigned j = a; j < b; j++) {
       float4 q4 = load(j);
       float3 rel = make_float3(q4.x - pos.x, q4.y - pos.y, q4.z - pos.z);
