@@ -160,11 +160,27 @@ __device__ __forceinline__ CellCull makeCull(float3 p, int3 g, float R, const Si
   return c;
 }
 
+// Asynchronous 16-byte copy global -> shared (cp.async, completion per
+// thread by commit groups).
+__device__ __forceinline__ void copyAsync16(float4 *dst, const float4 *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(
+                   (unsigned)__cvta_generic_to_shared(dst)),
+               "l"(__cvta_generic_to_global(src))
+               : "memory");
+}
+__device__ __forceinline__ void copyAsyncCommit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int kPending>
+__device__ __forceinline__ void copyAsyncWait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(kPending) : "memory");
+}
+
 // Per-thread queue of near partners (shared memory, entry q of thread t at
 // [q * kQueueStride + t]).
 constexpr int kQueueLen = 16;
 constexpr int kQueueStride = 128;
-constexpr int kStageLen = 128;  // staged partner positions per warp (collide row windows)
+constexpr int kStageLen = 128;  // staged partner positions per warp row buffer
 
 // The 27-cell loop with cell tables and positions read from global memory,
 // in two phases.  The scan over candidates only tests the squared distance
@@ -241,56 +257,12 @@ __device__ __forceinline__ float3 neighbourForceGlobal(
     }
   };
   auto loadGlobal = [&](unsigned j) { return ldg4(sortedPos + j); };
-  const unsigned lane = threadIdx.x & 31u;
-#pragma unroll 1
-  for (int row = 0; row < 9; row++) {
+  // one row's three cells one by one (the x wrap, Morton order or the split
+  // cellStart/cellEnd tables)
+  auto cellRow = [&](int row) {
     const int z = row / 3 - 1, y = row % 3 - 1;
     const float rowD2 = CellCull::pick(z, cc.zl, cc.zh) + CellCull::pick(y, cc.yl, cc.yh);
-    const bool rowLive = rowD2 <= cullR2;
-    const bool useL = rowD2 + CellCull::pick(-1, cc.xl, cc.xh) <= cullR2;
-    const bool useR = rowD2 + CellCull::pick(1, cc.xl, cc.xh) <= cullR2;
-    if (kPrefix && !mortonOrder(P)) {
-      const unsigned gxm = P.gridSize[0] - 1u;
-      const unsigned xm = (unsigned)(g.x) & gxm;
-      const bool merged = xm >= 1u && xm < gxm;
-      // no x wrap: the row's three cells are consecutive hashes, one range
-      unsigned a = 0, b = 0, o1 = 0, o2 = 0;
-      if (merged && rowLive) {
-        const unsigned h0 = gridHash(g.x - 1, g.y + y, g.z + z, P);
-        const unsigned o0 = __ldg(cells.off + h0);
-        o1 = __ldg(cells.off + h0 + 1);
-        o2 = __ldg(cells.off + h0 + 2);
-        const unsigned o3 = __ldg(cells.off + h0 + 3);
-        a = useL ? o0 : o1;
-        b = min(useR ? o3 : o2, n);
-      }
-      if (stage) {
-        // The lanes of a warp are consecutive sorted particles, mostly in
-        // one grid row: their ranges of this neighbour row overlap.  The
-        // warp copies the union into shared memory with coalesced loads and
-        // every lane scans its own range from there.  `live` is every lane
-        // of the warp that calls this function (fixed by a ballot before
-        // the call): all of them take part in each row's reductions, so a
-        // row's copy is never written while a group of lanes that fell
-        // behind (in a drain, or in a row scanned from global memory) still
-        // reads the previous one.
-        const unsigned lo = __reduce_min_sync(live, a < b ? a : 0xffffffffu);
-        const unsigned hi = __reduce_max_sync(live, a < b ? b : 0u);
-        if (lo < hi && hi - lo <= (unsigned)kStageLen) {
-          const unsigned rank = __popc(live & ((1u << lane) - 1u)), lanes = __popc(live);
-          for (unsigned t = rank; t < hi - lo; t += lanes) stage[t] = ldg4(sortedPos + lo + t);
-          __syncwarp(live);
-          scanRange(a, b, row * 3, o1, o2, [&](unsigned j) { return stage[j - lo]; });
-          __syncwarp(live);  // the copy is reused by the next row
-        } else if (merged) {
-          scanRange(a, b, row * 3, o1, o2, loadGlobal);
-        }
-      } else if (merged) {
-        scanRange(a, b, row * 3, o1, o2, loadGlobal);
-      }
-      if (merged) continue;
-    }
-    if (!rowLive) continue;
+    if (rowD2 > cullR2) return;
     unsigned h[3], start[3], end[3];
 #pragma unroll
     for (int x = 0; x < 3; x++) {
@@ -321,6 +293,89 @@ __device__ __forceinline__ float3 neighbourForceGlobal(
           qc[qn * kQueueStride] = (unsigned char)(row * 3 + x);
           ++qn;
         }
+      }
+    }
+  };
+  const bool linear = kPrefix && !mortonOrder(P);
+  const unsigned gxm = P.gridSize[0] - 1u;
+  const unsigned xm = (unsigned)(g.x) & gxm;
+  // no x wrap: a row's three cells are consecutive hashes, one range
+  const bool merged = linear && xm >= 1u && xm < gxm;
+  // row `row`'s merged range [a, b), split into its cells at o1 and o2
+  // (a == b: nothing to scan)
+  auto rowRange = [&](int row, unsigned &a, unsigned &b, unsigned &o1, unsigned &o2) {
+    const int z = row / 3 - 1, y = row % 3 - 1;
+    const float rowD2 = CellCull::pick(z, cc.zl, cc.zh) + CellCull::pick(y, cc.yl, cc.yh);
+    a = b = o1 = o2 = 0u;
+    if (merged && rowD2 <= cullR2) {
+      const unsigned h0 = gridHash(g.x - 1, g.y + y, g.z + z, P);
+      const unsigned o0 = __ldg(cells.off + h0);
+      o1 = __ldg(cells.off + h0 + 1);
+      o2 = __ldg(cells.off + h0 + 2);
+      const unsigned o3 = __ldg(cells.off + h0 + 3);
+      a = rowD2 + cc.xl <= cullR2 ? o0 : o1;
+      b = min(rowD2 + cc.xh <= cullR2 ? o3 : o2, n);
+    }
+  };
+  if (linear && stage) {
+    // The lanes of a warp are consecutive sorted particles, mostly in one
+    // grid row: their ranges of a neighbour row overlap.  The warp copies
+    // the union into shared memory with asynchronous 16-byte copies, and
+    // every lane scans its own range from there.  The copy of row r + 1 is
+    // issued before row r is scanned (two buffers of kStageLen), so it
+    // arrives while row r is scanned.  `live` is every lane of the warp that
+    // calls this function (fixed by a ballot before the call): all of them
+    // take part in each row's reductions and barriers, so a buffer is never
+    // refilled while a lane still reads it.
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned rank = __popc(live & ((1u << lane) - 1u)), lanes = __popc(live);
+    auto issue = [&](unsigned a, unsigned b, float4 *buf, unsigned &lo) {
+      lo = __reduce_min_sync(live, a < b ? a : 0xffffffffu);
+      const unsigned hi = __reduce_max_sync(live, a < b ? b : 0u);
+      const bool staged = lo < hi && hi - lo <= (unsigned)kStageLen;
+      if (staged)
+        for (unsigned t = rank; t < hi - lo; t += lanes) copyAsync16(buf + t, sortedPos + lo + t);
+      copyAsyncCommit();
+      return staged;  // false: the row is read from global memory
+    };
+    unsigned a0, b0, s10, s20, lo0;
+    rowRange(0, a0, b0, s10, s20);
+    bool st0 = issue(a0, b0, stage, lo0);
+#pragma unroll 1
+    for (int row = 0; row < 9; row++) {
+      unsigned a1 = 0, b1 = 0, s11 = 0, s21 = 0, lo1 = 0;
+      bool st1 = false;
+      if (row < 8) {
+        rowRange(row + 1, a1, b1, s11, s21);
+        st1 = issue(a1, b1, stage + ((row + 1) & 1) * kStageLen, lo1);
+        copyAsyncWait<1>();  // this lane's copies of row `row` have landed
+      } else {
+        copyAsyncWait<0>();
+      }
+      __syncwarp(live);  // and every other lane's
+      const float4 *buf = stage + (row & 1) * kStageLen;
+      if (st0)
+        scanRange(a0, b0, row * 3, s10, s20, [&](unsigned j) { return buf[j - lo0]; });
+      else if (merged)
+        scanRange(a0, b0, row * 3, s10, s20, loadGlobal);
+      if (!merged) cellRow(row);
+      __syncwarp(live);  // buffer row & 1 is refilled for row + 2
+      a0 = a1;
+      b0 = b1;
+      s10 = s11;
+      s20 = s21;
+      lo0 = lo1;
+      st0 = st1;
+    }
+  } else {
+#pragma unroll 1
+    for (int row = 0; row < 9; row++) {
+      if (merged) {
+        unsigned a, b, o1, o2;
+        rowRange(row, a, b, o1, o2);
+        scanRange(a, b, row * 3, o1, o2, loadGlobal);
+      } else {
+        cellRow(row);
       }
     }
   }
@@ -412,7 +467,7 @@ kCollideGlobal(float4 *__restrict__ newVel, const float4 *__restrict__ sortedPos
                CrowdList crowd, unsigned *status, bool stageRows) {
   __shared__ unsigned qj[kQueueLen * kQueueStride];
   __shared__ unsigned char qc[kQueueLen * kQueueStride];
-  __shared__ float4 sStage[4][kStageLen];
+  __shared__ float4 sStage[4][2 * kStageLen];  // two row buffers per warp
   const SimParams &P = kp.p;
   const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
   // every lane of the warp reaches the ballot below (the block is whole
