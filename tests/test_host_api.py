@@ -1,6 +1,6 @@
-"""Host-side pieces that need no GPU: the VTK particle writer, the C++
+"""Host-side pieces that need no GPU: the VTK particle writers, the C++
 particledem interface header (compiles and links against libfcdem.so), the
-scene generators."""
+scene generators, the collide configuration table."""
 import ctypes as C
 import os
 import subprocess
@@ -59,18 +59,25 @@ def test_gpu_particle_file_is_the_reference_format(tmp_path):
 
 
 def test_particledem_header_compiles_and_links():
+    """A program on fcdem_i3d.h alone (the i3d container types declared there,
+    no reference tree) resolves every particledem function of
+    cuda_addon/particledem.cuh:11-26 in libfcdem.so."""
     from fullc0ntact_gb300 import _native
     src = r'''
-#include "fcdem_particledem.h"
+#include "fcdem_i3d.h"
 int main() {
-  fcdem::HashGrid hg; fcdem::ParticleWorld pw;
-  if (hg.size_ != 0 || pw.size_ != 0) return 1;
+  i3d::HashGrid<float, i3d::cpu> hg;
+  i3d::ParticleWorld<float, i3d::cpu> pw;
+  (void)hg; (void)pw;
   /* no GPU work: only check that every call resolves */
-  void (*a)(fcdem::HashGrid &, fcdem::ParticleWorld &) = fcdem::calcHash;
-  void (*b)(fcdem::HashGrid &) = fcdem::sortParticles;
-  void (*c)(fcdem::HashGrid &, fcdem::ParticleWorld &) = fcdem::reorderDataAndFindCellStart;
-  void (*d)(fcdem::HashGrid &, fcdem::ParticleWorld &) = fcdem::evalForces;
-  return (a && b && c && d) ? 0 : 2;
+  void (*a)(i3d::HashGrid<float, i3d::cpu> &, i3d::ParticleWorld<float, i3d::cpu> &) = calcHash;
+  void (*b)(i3d::HashGrid<float, i3d::cpu> &) = sortParticles;
+  void (*c)(i3d::HashGrid<float, i3d::cpu> &, i3d::ParticleWorld<float, i3d::cpu> &) =
+      reorderDataAndFindCellStart;
+  void (*d)(i3d::HashGrid<float, i3d::cpu> &, i3d::ParticleWorld<float, i3d::cpu> &) = evalForces;
+  void (*e)(float *, float *, float, unsigned int) = integrateSystem;
+  void (*f)() = cuda_clean;
+  return (a && b && c && d && e && f && cuda_init) ? 0 : 2;
 }'''
     with tempfile.TemporaryDirectory() as tmp:
         cpp = os.path.join(tmp, "t.cpp")
