@@ -427,8 +427,9 @@ def measure_torus_obstacle(n: int, steps: int, dev: int) -> dict:
     """Spheres falling onto the torus obstacle (128^3 distance map) through
     the fused unified-memory step: plain (exact map query for every particle
     in the map box) and with the neural SDF culling the query (3 -> 64 -> 64
-    -> 64 -> 1 SiLU network trained on 2M map samples; skin 2 radii).  Both
-    from the same initial state; CUDA events on the stream."""
+    -> 64 -> 1 SiLU network trained on 2M map samples; skin 2 radii), per
+    particle and per 32-particle tile.  All from the same initial state;
+    CUDA events on the stream."""
     import ctypes as C
     import torch
     from fullc0ntact_gb300 import dem, scenes, sdf
@@ -481,10 +482,12 @@ def measure_torus_obstacle(n: int, steps: int, dev: int) -> dict:
     lib.fcdemGetStageTimes.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_uint), C.c_int]
     out = {}
     finals = {}
-    for mode in ("plain", "neural"):
+    lip, lip_raw = sdf.calibrate_lipschitz(net, [dmap], shaped=False)
+    for mode in ("plain", "neural", "neural_tiles"):
+        net.set_tile_culling(lip if mode == "neural_tiles" else 0.0)
         us = dem.UmScene(sc, dmap, f"cuda:{dev}")
         counter = torch.zeros(1, dtype=torch.int32, device=us.pos.device)
-        kw = dict(net=net, skin=skin, exact_counter=counter) if mode == "neural" else {}
+        kw = dict(net=net, skin=skin, exact_counter=counter) if mode != "plain" else {}
         us.update(3, **kw)  # warm-up
         us.pos.copy_(torch.from_numpy(sc["pos"]))
         us.vel.copy_(torch.from_numpy(sc["vel"]))
@@ -512,11 +515,13 @@ def measure_torus_obstacle(n: int, steps: int, dev: int) -> dict:
         out[mode] = {"value": n * steps / (ms / 1e3), "ms_per_step": ms / steps,
                      "stage_ms_per_step": {names[k]: (st[k] / steps if cnt[k] else None)
                                            for k in range(5)}}
-        if mode == "neural":
+        if mode != "plain":
             out[mode]["exact_map_queries_per_step"] = exact / steps
         del us
     same = all(torch.equal(a.view(torch.int32), b.view(torch.int32))
                for a, b in zip(finals["plain"], finals["neural"]))
+    same_t = all(torch.equal(a.view(torch.int32), b.view(torch.int32))
+                 for a, b in zip(finals["plain"], finals["neural_tiles"]))
     # The same scene over finer analytic maps of the torus (the map grows
     # past the 129 MB L2): what an exact query costs against the network as
     # the map leaves the cache.  The network is the one trained above.
@@ -525,9 +530,10 @@ def measure_torus_obstacle(n: int, steps: int, dev: int) -> dict:
         big = dem.DistanceMap.torus(0.3, 0.1, cpa, 0.05)
         row = {"cells_per_axis": cpa, "map_mb": float(np.prod(np.array(big.cells) + 1)) * 16 / 1e6}
         res = {}
-        for mode in ("exact", "neural"):
+        for mode in ("exact", "neural", "neural_tiles"):
+            net.set_tile_culling(lip if mode == "neural_tiles" else 0.0)
             us = dem.UmScene(sc, big, f"cuda:{dev}")
-            kw = dict(net=net, skin=skin) if mode == "neural" else {}
+            kw = dict(net=net, skin=skin) if mode != "exact" else {}
             us.update(3, **kw)
             us.pos.copy_(torch.from_numpy(sc["pos"]))
             us.vel.copy_(torch.from_numpy(sc["vel"]))
@@ -541,11 +547,15 @@ def measure_torus_obstacle(n: int, steps: int, dev: int) -> dict:
             res[mode] = (us.pos.clone(), us.vel.clone())
             del us
         row["neural_over_exact"] = row["exact_ms_per_step"] / row["neural_ms_per_step"]
+        row["neural_tiles_over_exact"] = (row["exact_ms_per_step"] /
+                                          row["neural_tiles_ms_per_step"])
         row["equal_final_state"] = all(torch.equal(a.view(torch.int32), b.view(torch.int32))
-                                       for a, b in zip(res["exact"], res["neural"]))
+                                       for k in ("neural", "neural_tiles")
+                                       for a, b in zip(res["exact"], res[k]))
         curve.append(row)
         del big, res
         torch.cuda.empty_cache()
+    net.set_tile_culling(0.0)
     return {"workload": f"{n} spheres r=1/256 falling onto a torus (R 0.3, r 0.1; mesh of "
                         "256 x 64 quads, 32768 triangles), 128-cell distance map built from the "
                         "mesh on the GPU, unified-memory step (calcHash, sort, reorder, "
@@ -555,6 +565,10 @@ def measure_torus_obstacle(n: int, steps: int, dev: int) -> dict:
             "plain_exact_map": out["plain"], "neural_sdf": out["neural"],
             "speedup": out["neural"]["value"] / out["plain"]["value"],
             "equal_final_state": bool(same),
+            "neural_sdf_tiles": dict(out["neural_tiles"], lipschitz_measured=lip_raw,
+                                     lipschitz_used=lip),
+            "speedup_tiles": out["neural_tiles"]["value"] / out["plain"]["value"],
+            "equal_final_state_tiles": bool(same_t),
             "map_size_curve": {"steps": 100, "maps": "analytic torus maps, 16 B per vertex",
                                "points": curve},
             "network": {"layers": "3-64-64-64-1 SiLU", "params": net.num_params,
@@ -573,8 +587,8 @@ def measure_batched_obstacles(num_scenes: int, steps: int, dev: int) -> dict:
     shape-conditioned network (11 -> 128 -> 128 -> 1) trained on samples of
     all maps.  Timed over the same job from the same initial state: the
     whole batch replayed from a CUDA graph with the network culling the map
-    query; the batch with exact queries; each scene stepped alone with exact
-    queries (the plain step)."""
+    query per particle, and per 32-slot tile; the batch with exact queries;
+    each scene stepped alone with exact queries (the plain step)."""
     import torch
     from fullc0ntact_gb300 import dem, scenes, sdf
     scs, obs, shape = scenes.batch_obstacle_scenes(num_scenes)
@@ -599,7 +613,12 @@ def measure_batched_obstacles(num_scenes: int, steps: int, dev: int) -> dict:
     pos0 = torch.from_numpy(np.concatenate([s["pos"] for s in scs]))
     vel0 = torch.from_numpy(np.concatenate([s["vel"] for s in scs]))
 
-    def timed_batch(use_net):
+    # culling per 32-slot tile: a Lipschitz bound of the prediction from
+    # held-out pairs of points
+    lip, lip_raw = sdf.calibrate_lipschitz(net, maps)
+
+    def timed_batch(use_net, tiles=False):
+        net.set_tile_culling(lip if tiles else 0.0)
         b = dem.Batch(scs, f"cuda:{dev}")
         b.set_obstacles(maps, shape, net if use_net else None, skin)
         b.update(steps, graph=True)  # records the graph (and warms up)
@@ -615,10 +634,14 @@ def measure_batched_obstacles(num_scenes: int, steps: int, dev: int) -> dict:
         return b, e0.elapsed_time(e1), b.exact_queries()
 
     bn, ms_n, ex_n = timed_batch(True)
+    bt, ms_t, ex_t = timed_batch(True, tiles=True)
+    net.set_tile_culling(0.0)
     bp, ms_p, ex_p = timed_batch(False)
     same = (torch.equal(bn.pos.view(torch.int32), bp.pos.view(torch.int32)) and
             torch.equal(bn.vel.view(torch.int32), bp.vel.view(torch.int32)))
-    del bn, bp
+    same_t = (torch.equal(bt.pos.view(torch.int32), bp.pos.view(torch.int32)) and
+              torch.equal(bt.vel.view(torch.int32), bp.vel.view(torch.int32)))
+    del bn, bp, bt
     torch.cuda.empty_cache()
     singles = []
     for k, sc in enumerate(scs):
@@ -650,11 +673,17 @@ def measure_batched_obstacles(num_scenes: int, steps: int, dev: int) -> dict:
             "steps": steps, "unit": UNIT,
             "batched_neural_graph": {"value": val_of(ms_n), "ms_per_step": ms_n / steps,
                                      "exact_map_queries_per_step": ex_n / steps},
+            "batched_neural_tiles_graph": {"value": val_of(ms_t), "ms_per_step": ms_t / steps,
+                                           "exact_map_queries_per_step": ex_t / steps,
+                                           "lipschitz_measured": lip_raw, "lipschitz_used": lip,
+                                           "equal_final_state_vs_exact": bool(same_t)},
             "batched_exact_graph": {"value": val_of(ms_p), "ms_per_step": ms_p / steps,
                                     "exact_map_queries_per_step": ex_p / steps},
             "plain_per_scene_exact": {"value": val_of(ms_s), "ms_per_step": ms_s / steps},
             "speedup_vs_plain": ms_s / ms_n,
+            "speedup_vs_plain_tiles": ms_s / ms_t,
             "network_effect_in_batch": ms_p / ms_n,
+            "network_effect_in_batch_tiles": ms_p / ms_t,
             "equal_final_state_neural_vs_exact": bool(same),
             "network": {"layers": "11-128-128-1 SiLU (8 one-hot shape codes)",
                         "params": net.num_params, "train_samples": 500_000 * len(maps),

@@ -232,7 +232,10 @@ void fcdemBatchSetObstacles(fcdemBatch *b, const fcdemDistanceMap *const *maps, 
   b->net = numMaps ? net : nullptr;
   b->skin = skin;
   if (numMaps == 0) return;
-  if (net) sdfHints(net, (b->n + 127) / 128);  // now, not while a graph is recorded
+  if (net) {  // now, not while a graph is recorded
+    sdfHints(net, (b->n + 127) / 128);
+    sdfPrepareTiles(net, b->n);
+  }
   std::vector<MapView> hv(numMaps);
   for (uint k = 0; k < numMaps; ++k) hv[k] = view(maps[k]);
   if (cudaMalloc(&b->maps, sizeof(MapView) * numMaps) != cudaSuccess ||
@@ -281,6 +284,9 @@ void fcdemBatchUpdate(fcdemBatch *b, float *pos, float *vel, float deltaTime, ui
     if (!b->captureStream &&
         !cudaOk(cudaStreamCreateWithFlags(&b->captureStream, cudaStreamNonBlocking)))
       return;
+    // the network's per-tile arrays are grown now, not while the graph is
+    // recorded (the culling mode may have changed since the obstacles were set)
+    if (b->net && !sdfPrepareTiles(b->net, b->n)) return;
     const cudaStream_t prev = curStream();
     fcdemSetStream(b->captureStream);
     cudaGraph_t graph = nullptr;

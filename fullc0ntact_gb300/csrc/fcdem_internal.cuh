@@ -232,6 +232,9 @@ bool batchObstacleIntegrate(const BatchScene *scenes, const unsigned *sceneOf, b
 // The network's per-tile culling hints for `tiles` tiles, allocated (and
 // cleared) when they grow; nullptr when they cannot be had.
 unsigned char *sdfHints(fcdemSdfNet *net, unsigned tiles);
+// The per-tile arrays of the network's culling per tile (when that is on)
+// for n slots, grown now; false when they cannot be had.
+bool sdfPrepareTiles(fcdemSdfNet *net, unsigned n);
 // Changes with every change of the network's weights or normalisation (a
 // recorded graph holds the values of its recording).
 unsigned sdfVersion(const fcdemSdfNet *net);

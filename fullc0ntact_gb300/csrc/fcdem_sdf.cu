@@ -667,6 +667,118 @@ struct TileHints {
   int refresh;
 };
 
+// Culling per tile (fcdemSdfSetTileCulling).  The network runs once per
+// tile of kCullTile consecutive slots, at the centre c of the box that
+// bounds the tile's particles in the map box (after this step's velocity
+// and position update), and the tile's exact queries are skipped when
+// pred(c) - lip * rho > skin, rho being the distance from c to the box's
+// corners.  With lip a Lipschitz bound of the network's prediction, every
+// particle p of such a tile has pred(p) >= pred(c) - lip * |p - c| > skin:
+// the per-particle rule would have skipped it as well.  Where the rule
+// does not cull, every particle of the tile in the map box is queried.  A
+// tile whose particles in the map box belong to scenes of different
+// obstacles is not culled.
+constexpr unsigned kCullTile = 32;
+struct TileCull {
+  const float4 *centre;  // per tile: c (x, y, z) and rho (w)
+  const int *shape;      // per tile: the obstacle's shape code; -1 none in the box, -2 mixed
+  const float *pred;     // per tile: the network's distance at c
+  float lip, skin;
+  __device__ __forceinline__ bool cull(unsigned tile) const {
+    return __ldg(shape + tile) >= 0 &&
+           __ldg(pred + tile) - lip * __ldg(&centre[tile].w) > skin;
+  }
+};
+
+// One warp per tile: the bounding box of the tile's advanced positions in
+// the map box (umAdvance: the arithmetic of the integrate that follows).
+// kBatch: slot i belongs to scene sceneOf[i] with its own parameters and
+// obstacle; otherwise every particle has kp and the map M.
+template <bool kBatch>
+__global__ void __launch_bounds__(256)
+kTileCentres(const BatchScene *__restrict__ scenes, const unsigned *__restrict__ sceneOf,
+             const MapView *__restrict__ maps, KParams kp, MapView M,
+             const float4 *__restrict__ pos, const float4 *__restrict__ vel, float dt,
+             unsigned n, float4 *__restrict__ centre, int *__restrict__ shapeOut) {
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const unsigned tiles = (n + kCullTile - 1) / kCullTile;
+  if (tile >= tiles) return;  // whole warps leave together
+  const unsigned i = tile * kCullTile + lane;
+  bool in = false;
+  int shape = -1;
+  float3 p = make_float3(0.0f, 0.0f, 0.0f);
+  if (i < n) {
+    const float4 p4 = __ldg(pos + i), v4 = __ldg(vel + i);
+    p = make_float3(p4.x, p4.y, p4.z);
+    float3 v = make_float3(v4.x, v4.y, v4.z);
+    if (kBatch) {
+      const BatchScene &S = scenes[__ldg(sceneOf + i)];
+      umAdvance(p, v, dt, S.p);
+      shape = S.shape;
+      in = shape >= 0 && inMapBox(maps[shape], p);
+    } else {
+      umAdvance(p, v, dt, kp.p);
+      shape = 0;
+      in = inMapBox(M, p);
+    }
+  }
+  const float inf = __int_as_float(0x7f800000);
+  float lx = in ? p.x : inf, ly = in ? p.y : inf, lz = in ? p.z : inf;
+  float hx = in ? p.x : -inf, hy = in ? p.y : -inf, hz = in ? p.z : -inf;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    lx = fminf(lx, __shfl_xor_sync(0xffffffffu, lx, o));
+    ly = fminf(ly, __shfl_xor_sync(0xffffffffu, ly, o));
+    lz = fminf(lz, __shfl_xor_sync(0xffffffffu, lz, o));
+    hx = fmaxf(hx, __shfl_xor_sync(0xffffffffu, hx, o));
+    hy = fmaxf(hy, __shfl_xor_sync(0xffffffffu, hy, o));
+    hz = fmaxf(hz, __shfl_xor_sync(0xffffffffu, hz, o));
+  }
+  const int smin = __reduce_min_sync(0xffffffffu, in ? shape : 0x7fffffff);
+  const int smax = __reduce_max_sync(0xffffffffu, in ? shape : -1);
+  if (lane == 0) {
+    if (smax < 0) {
+      centre[tile] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      shapeOut[tile] = -1;
+    } else {
+      const float ex = hx - lx, ey = hy - ly, ez = hz - lz;
+      // rho with a margin for the roundings of the centre and of the root
+      const float rho = 0.5f * sqrtf(ex * ex + ey * ey + ez * ez) * 1.0001f + 1e-6f;
+      centre[tile] = make_float4(0.5f * (lx + hx), 0.5f * (ly + hy), 0.5f * (lz + hz), rho);
+      shapeOut[tile] = smin == smax ? smin : -2;
+    }
+  }
+}
+
+// kIntegrateDistMap's step with the map query of culled tiles skipped.
+template <bool kCount>
+__global__ void __launch_bounds__(256)
+kIntegrateTileCull(float4 *__restrict__ pos, float4 *__restrict__ vel, float dt, unsigned n,
+                   KParams kp, MapView M, TileCull tc, unsigned *exact,
+                   unsigned *__restrict__ hashOut, unsigned *__restrict__ rankOut,
+                   unsigned *__restrict__ cnt, unsigned *__restrict__ tileCnt) {
+  const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const SimParams &P = kp.p;
+  const float4 p4 = pos[i], v4 = vel[i];
+  float3 p = make_float3(p4.x, p4.y, p4.z), v = make_float3(v4.x, v4.y, v4.z);
+  const float r = kp.radiusFromW ? p4.w : P.particleRadius;
+  umAdvance(p, v, dt, P);
+  const bool test = inMapBox(M, p) && !tc.cull(i / kCullTile);
+  if (test && exact) atomicAdd(exact, 1u);
+  umBoundary(M, test, r, P.boundaryDamping, p, v);
+  if (kCount) {  // the next step's calcHash and cell count
+    const int3 gp = gridPos(p.x, p.y, p.z, P);
+    const unsigned h = gridHash(gp.x, gp.y, gp.z, P);
+    hashOut[i] = h;
+    rankOut[i] = atomicAdd(cnt + h, 1u);
+    countTile(tileCnt, h >> 12);
+  }
+  pos[i] = make_float4(p.x, p.y, p.z, p4.w);
+  vel[i] = make_float4(v.x, v.y, v.z, p4.w);
+}
+
 // d_integrateSystem + d_checkBoundaryDistMap (kIntegrateDistMap's
 // arithmetic) with the map query skipped where the network predicts a
 // distance above `skin`: a point outside the map box reads 5.0 from the map
@@ -749,13 +861,14 @@ __device__ __forceinline__ void boxClamp(float3 &p, float3 &v, float r, float bd
 // doCount the next global cell id and count.  kNet: a tile of 128 with a
 // particle in its obstacle's map box runs the network (the scene's shape as
 // the one-hot code) and only particles predicted within `skin` query the map.
+// Without kNet, tc (when set) holds the decisions of the culling per tile.
 template <int H, int L, bool kNet, bool kW>
 __global__ void __launch_bounds__(128)
 kBatchObstacle(const BatchScene *__restrict__ scenes, const unsigned *__restrict__ sceneOf,
                const MapView *__restrict__ maps, SdfView net, float skin,
                const float4 *__restrict__ inPos, float4 *__restrict__ pos,
                float4 *__restrict__ vel, float dt, unsigned n, UmCount count, int doCount,
-               unsigned *exact, TileHints hints, unsigned *status) {
+               unsigned *exact, TileHints hints, TileCull tc, unsigned *status) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   SdfTileSmem<H, L> &sm = *reinterpret_cast<SdfTileSmem<H, L> *>(smraw);
   if (kNet) sdfTileSetup<H, L>(sm, net);
@@ -791,7 +904,9 @@ kBatchObstacle(const BatchScene *__restrict__ scenes, const unsigned *__restrict
         break;
       }
     }
-    const bool test = inBox && (!useNet || !(dPred > skin));
+    // without the network in the kernel: the tiles' decisions (TileCull), if any
+    const bool test = inBox && (!useNet || !(dPred > skin)) &&
+                      (kNet || !tc.shape || !tc.cull(i / kCullTile));
     if (kNet && useNet && hints.h) {
       const int nIn = __syncthreads_count(inBox), nTest = __syncthreads_count(test);
       if (threadIdx.x == 0) hints.h[tile] = 2 * nTest > nIn ? 1 : 0;
@@ -846,6 +961,9 @@ struct fcdemSdfNet {
   unsigned version = 0;  // bumped whenever the weights or the normalisation change
   unsigned char *hints = nullptr;  // per-tile culling hints (TileHints)
   unsigned hintTiles = 0;
+  float tileLip = 0.0f;          // > 0: cull per tile of kCullTile slots (TileCull)
+  void *tileBuf = nullptr;       // TileCull's centres, shapes and predictions
+  unsigned tileCap = 0;          // tiles tileBuf holds
 };
 
 namespace fcdem {
@@ -879,6 +997,7 @@ void freeNet(fcdemSdfNet *net) {
   cudaFree(net->loss);
   cudaFree(net->w16);
   cudaFree(net->hints);
+  cudaFree(net->tileBuf);
   delete net;
 }
 
@@ -1039,7 +1158,7 @@ template <int H, int L, bool kNet, bool kW>
 bool launchBatchObstacle(fcdemSdfNet *net, const BatchScene *scenes, const unsigned *sceneOf,
                          const MapView *maps, float skin, const float4 *inPos, float4 *pos,
                          float4 *vel, float dt, unsigned n, const UmCount *count,
-                         unsigned *exact, TileHints hints) {
+                         unsigned *exact, TileHints hints, TileCull tc = TileCull{}) {
   unsigned grid = (n + 127) / 128;
   size_t smem = 0;
   SdfView v{};
@@ -1052,7 +1171,7 @@ bool launchBatchObstacle(fcdemSdfNet *net, const BatchScene *scenes, const unsig
   }
   kBatchObstacle<H, L, kNet, kW><<<grid, 128, smem, curStream()>>>(
       scenes, sceneOf, maps, v, skin, inPos, pos, vel, dt, n, count ? *count : UmCount{},
-      count ? 1 : 0, exact, hints, ctx().dStatus);
+      count ? 1 : 0, exact, hints, tc, ctx().dStatus);
   return launchOk();
 }
 
@@ -1081,11 +1200,78 @@ unsigned char *sdfHints(fcdemSdfNet *net, unsigned tiles) {
   return net->hints;
 }
 
+// The net's per-tile arrays of the culling per tile, for n slots (grown on
+// demand); nullptr when they cannot be had.
+bool sdfTileBuffers(fcdemSdfNet *net, unsigned n, TileCull &tc) {
+  const unsigned tiles = (n + kCullTile - 1) / kCullTile;
+  if (!net->tileBuf || net->tileCap < tiles) {
+    if (!cudaOk(cudaDeviceSynchronize())) return false;
+    cudaFree(net->tileBuf);
+    net->tileBuf = nullptr;
+    net->tileCap = 0;
+    if (cudaMalloc(&net->tileBuf, (size_t)tiles * 24) != cudaSuccess) {
+      cudaGetLastError();
+      setError(FCDEM_ERR_ALLOC);
+      return false;
+    }
+    net->tileCap = tiles;
+  }
+  float4 *centre = (float4 *)net->tileBuf;
+  int *shape = (int *)(centre + net->tileCap);
+  float *pred = (float *)(shape + net->tileCap);
+  tc = TileCull{centre, shape, pred, net->tileLip, 0.0f};
+  return true;
+}
+
+bool sdfPrepareTiles(fcdemSdfNet *net, unsigned n) {
+  TileCull tc{};
+  return !net || !(net->tileLip > 0.0f) || n == 0 || sdfTileBuffers(net, n, tc);
+}
+
+// The tiles' centres and the network's predictions there (culling per tile).
+template <bool kBatch>
+bool tileDecisions(fcdemSdfNet *net, const BatchScene *scenes, const unsigned *sceneOf,
+                   const MapView *maps, const KParams &kp, const MapView &M,
+                   const float4 *inPos, const float4 *vel, float dt, unsigned n, float skin,
+                   TileCull &tc) {
+  if (!sdfTileBuffers(net, n, tc)) return false;
+  tc.skin = skin;
+  const unsigned tiles = (n + kCullTile - 1) / kCullTile;
+  kTileCentres<kBatch><<<(tiles * 32 + 255) / 256, 256, 0, curStream()>>>(
+      scenes, sceneOf, maps, kp, M, inPos, vel, dt, n, const_cast<float4 *>(tc.centre),
+      const_cast<int *>(tc.shape));
+  if (!launchOk()) return false;
+  // the shape codes go to the network too (a negative code: no one-hot input)
+  const int *shapes = kBatch ? tc.shape : nullptr;
+  const int H = net->lay.H, L = net->lay.L;
+  float *pred = const_cast<float *>(tc.pred);
+  if (H == 64 && L == 3) return launchInfer<64, 3>(net, tc.centre, shapes, tiles, pred);
+  if (H == 64 && L == 2) return launchInfer<64, 2>(net, tc.centre, shapes, tiles, pred);
+  if (H == 128 && L == 2) return launchInfer<128, 2>(net, tc.centre, shapes, tiles, pred);
+  if (H == 128 && L == 3) return launchInfer<128, 3>(net, tc.centre, shapes, tiles, pred);
+  setError(FCDEM_ERR_INVALID_VALUE);
+  return false;
+}
+
 bool batchObstacleIntegrate(const BatchScene *scenes, const unsigned *sceneOf, bool radiusFromW,
                             const MapView *maps, fcdemSdfNet *net, float skin,
                             const float4 *inPos, float4 *pos, float4 *vel, float dt,
                             unsigned n, const UmCount *count, unsigned *exact, unsigned step) {
   if (n == 0) return true;
+  if (net && net->tileLip > 0.0f) {
+    if (!packWeights(net)) return false;
+    TileCull tc{};
+    if (!tileDecisions<true>(net, scenes, sceneOf, maps, KParams{}, MapView{}, inPos, vel, dt,
+                             n, skin, tc))
+      return false;
+    const TileHints none{nullptr, 1};
+    return radiusFromW
+               ? launchBatchObstacle<64, 3, false, true>(net, scenes, sceneOf, maps, skin, inPos,
+                                                         pos, vel, dt, n, count, exact, none, tc)
+               : launchBatchObstacle<64, 3, false, false>(net, scenes, sceneOf, maps, skin,
+                                                          inPos, pos, vel, dt, n, count, exact,
+                                                          none, tc);
+  }
   if (!net) {
     const TileHints none{nullptr, 1};
     return radiusFromW
@@ -1121,6 +1307,21 @@ bool sdfIntegrate(fcdemSdfNet *net, float4 *pos, float4 *vel, float dt, unsigned
   if (!packWeights(net)) return false;
   const int H = net->lay.H, L = net->lay.L;
   const MapView M = view(map);
+  if (net->tileLip > 0.0f) {
+    if (n == 0) return true;
+    TileCull tc{};
+    if (!tileDecisions<false>(net, nullptr, nullptr, nullptr, kp, M, pos, vel, dt, n, skin, tc))
+      return false;
+    const unsigned blocks = (n + 255) / 256;
+    if (count)
+      kIntegrateTileCull<true><<<blocks, 256, 0, curStream()>>>(
+          pos, vel, dt, n, kp, M, tc, exact, count->hash, count->rank, count->cnt,
+          count->tileCnt);
+    else
+      kIntegrateTileCull<false><<<blocks, 256, 0, curStream()>>>(
+          pos, vel, dt, n, kp, M, tc, exact, nullptr, nullptr, nullptr, nullptr);
+    return launchOk();
+  }
   // step < 0: a lone call, no hints
   const TileHints hints{step < 0 ? nullptr : sdfHints(net, (n + 127) / 128),
                         (step < 0 || step % (int)kHintRefresh == 0) ? 1 : 0};
@@ -1213,6 +1414,15 @@ void fcdemSdfSetNormalization(fcdemSdfNet *net, const float shift[3], const floa
   }
   net->outScale = outScale;
   net->version++;
+}
+
+void fcdemSdfSetTileCulling(fcdemSdfNet *net, float lipschitz) {
+  if (!net || !(lipschitz >= 0.0f)) {
+    setError(FCDEM_ERR_INVALID_VALUE);
+    return;
+  }
+  net->tileLip = lipschitz;
+  net->version++;  // a recorded batch graph holds the launches of the other mode
 }
 
 void fcdemSdfGetNormalization(const fcdemSdfNet *net, float shift[3], float scale[3],

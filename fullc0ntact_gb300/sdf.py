@@ -34,6 +34,7 @@ _SIGS = {
     "fcdemSdfTrainSamples": (f32, [vp, vp, vp, u32, u32, u32, f32, f32]),
     "fcdemSdfEvalF32": (None, [vp, vp, vp, u32, vp]),
     "fcdemSdfInfer": (None, [vp, vp, vp, u32, vp]),
+    "fcdemSdfSetTileCulling": (None, [vp, f32]),
     "fcdemUM_integrateSystemSdf": (None, [vp, vp, f32, u32, vp, vp, f32, vp]),
 }
 for _name, (_res, _args) in _SIGS.items():
@@ -122,6 +123,12 @@ class SdfNet:
         check("fcdemSdfInfer")
         return d
 
+    def set_tile_culling(self, lipschitz: float) -> None:
+        """0: cull the map query per particle; > 0: per tile of 32 slots with
+        this Lipschitz bound of the prediction (fcdemSdfSetTileCulling)."""
+        lib.fcdemSdfSetTileCulling(self._h, float(lipschitz))
+        check("fcdemSdfSetTileCulling")
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h:
@@ -203,3 +210,35 @@ def calibrate_skin(net: SdfNet, maps: list, radius: float, samples_per_map: int 
         if bool(touching.any()):
             p_max = max(p_max, float(pred[touching].max()))
     return max(2.0 * radius, p_max + margin * max(p_max - radius, 0.0)), p_max
+
+
+def calibrate_lipschitz(net: SdfNet, maps: list, pairs_per_map: int = 500_000,
+                        seed: int = 400, shaped: bool = True, safety: float = 1.5,
+                        min_step: float = 0.004, max_step: float = 0.08) -> tuple:
+    """A Lipschitz bound of the network's BF16 prediction (the one the culling
+    uses), measured on held-out pairs of points of every map box: x from the
+    map's own samples (half of them near the surface), y = x + a step of
+    random direction and length U[min_step, max_step], kept in the box.
+    L = max |pred(x) - pred(y)| / |x - y|; returns (safety * L, L)."""
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    lip = 0.0
+    for k, m in enumerate(maps):
+        if shaped:
+            x, sh = samples(m, pairs_per_map, 0.5, 0.03, seed=seed + k, shape=k)
+        else:
+            x, sh = samples(m, pairs_per_map, 0.5, 0.03, seed=seed + k), None
+        u = torch.randn(pairs_per_map, 3, generator=g, device="cuda")
+        u = u / u.norm(dim=1, keepdim=True)
+        step = min_step + (max_step - min_step) * torch.rand(pairs_per_map, 1, generator=g,
+                                                             device="cuda")
+        y = x.clone()
+        y[:, :3] = x[:, :3] + u * step
+        lo = torch.as_tensor(m.vmin, device="cuda")
+        hi = torch.as_tensor(m.vmax, device="cuda")
+        keep = ((y[:, :3] >= lo) & (y[:, :3] <= hi)).all(dim=1)
+        x, y = x[keep].contiguous(), y[keep].contiguous()
+        shk = sh[keep].contiguous() if sh is not None else None
+        px, py = net.infer(x, shk), net.infer(y, shk)
+        ratio = (px - py).abs() / (x[:, :3] - y[:, :3]).norm(dim=1)
+        lip = max(lip, float(ratio.max()))
+    return safety * lip, lip

@@ -417,6 +417,19 @@ void fcdemSdfEvalF32(fcdemSdfNet *net, const float *points4, const int *shapes, 
                      float *d);
 void fcdemSdfInfer(fcdemSdfNet *net, const float *points4, const int *shapes, uint n,
                    float *d);
+/* How the network culls the map query (fcdemUM_update, fcdemUM_integrateSystemSdf,
+ * batch obstacles).  lipschitz 0 (the default): per particle, the network
+ * runs on every 128-slot tile with a particle in the map box and a particle
+ * is queried when its prediction is at most `skin`.  lipschitz > 0: per tile
+ * of 32 slots, the network runs once, at the centre c of the box bounding
+ * the tile's particles in the map box (rho: c to the box's corners), and the
+ * tile's queries are skipped when pred(c) - lipschitz * rho > skin; otherwise
+ * each of its particles in the map box is queried.  `lipschitz` must bound
+ * the network's prediction's Lipschitz constant (sdf.calibrate_lipschitz
+ * measures one); then a tile is skipped only where the per-particle rule
+ * would skip each of its particles.  A batch replayed from a graph records
+ * again after a change. */
+void fcdemSdfSetTileCulling(fcdemSdfNet *net, float lipschitz);
 /* `steps` unified-memory DEM steps (CollisionPipeline<dem_gpu_unified>::
  * startPipeline, dempipeline.hpp:113-120: calcHash, sortParticles,
  * reorderDataAndFindCellStart, evalForces, integrateSystem with the map

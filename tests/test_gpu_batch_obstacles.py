@@ -123,3 +123,34 @@ def test_graph_records_again_after_the_network_changes():
     after = b.exact_queries(reset=True)
     print("exact queries per 10 steps before / after", before, after)
     assert after < 0.2 * before
+
+
+def test_tile_culling_is_exact_and_queries_less():
+    """Culling per tile (fcdemSdfSetTileCulling): the shape network runs once
+    per 32-slot tile at the centre of the tile's particles in the map box,
+    with a Lipschitz bound measured on held-out pairs.  40 batched steps end
+    in the bits of the exact maps, with fewer exact queries."""
+    from fullc0ntact_gb300 import dem, sdf
+    scs, obs, shape = _small_obstacle_batch(num_scenes=8, seed=6)
+    maps = sdf.obstacle_maps(obs, 128)
+    net, loss = sdf.shape_net(maps)
+    r_max = 1.0 / 256.0
+    skin, _ = sdf.calibrate_skin(net, maps, r_max, seed=300)
+    lip, lip_raw = sdf.calibrate_lipschitz(net, maps)
+    print("skin", skin, "lipschitz", lip_raw, "used", lip)
+    assert 0.5 < lip_raw < 4.0  # a distance field's slope is 1
+    net.set_tile_culling(lip)
+    a, b = dem.Batch(scs), dem.Batch(scs)
+    a.set_obstacles(maps, shape)
+    b.set_obstacles(maps, shape, net=net, skin=skin)
+    steps = 40
+    a.update(steps, graph=True)
+    b.update(steps, graph=True)
+    dem.check("batch, tile culling")
+    np.testing.assert_array_equal(a.pos.cpu().numpy().view(np.uint32),
+                                  b.pos.cpu().numpy().view(np.uint32))
+    np.testing.assert_array_equal(a.vel.cpu().numpy().view(np.uint32),
+                                  b.vel.cpu().numpy().view(np.uint32))
+    ea, eb = a.exact_queries(), b.exact_queries()
+    print("exact queries exact/tile-culled", ea, eb)
+    assert 0 < eb < ea, (ea, eb)

@@ -57,3 +57,30 @@ def test_um_update_with_sdf_culling_equals_exact_map():
     dem.check("um update sdf")
     _same(_state(a), _state(b))
     assert 0 < int(counter.item()) < 0.5 * steps * sc["pos"].shape[0]
+
+
+def test_um_update_with_sdf_tile_culling_equals_exact_map():
+    """The same step with the network culling per 32-particle tile (a
+    Lipschitz bound measured on held-out pairs): the state of the exact map,
+    bit for bit, with fewer exact queries than particles in the map box."""
+    from fullc0ntact_gb300 import dem, scenes, sdf
+    dmap = dem.DistanceMap.torus(0.3, 0.1, 128, 0.05)
+    net = sdf.SdfNet(3, 64, 3, seed=5)
+    net.normalize_to(dmap)
+    net.train(sdf.samples(dmap, 2_000_000, 0.6, 0.05, seed=21), epochs=20, batch=2048,
+              lr=5e-3, band=0.02)
+    sc = scenes.torus_fall_scene(200_000, z0=0.105)
+    r = sc["radius"]
+    skin, _ = sdf.calibrate_skin(net, [dmap], r, shaped=False)
+    skin = max(skin, 2.0 * r)
+    lip, lip_raw = sdf.calibrate_lipschitz(net, [dmap], shaped=False)
+    print("skin", skin, "lipschitz", lip_raw)
+    net.set_tile_culling(lip)
+    a, b = dem.UmScene(sc, dmap), dem.UmScene(sc, dmap)
+    counter = torch.zeros(1, dtype=torch.int32, device="cuda")
+    steps = 30
+    a.update(steps)
+    b.update(steps, net=net, skin=skin, exact_counter=counter)
+    dem.check("um update, tile culling")
+    _same(_state(a), _state(b))
+    assert 0 < int(counter.item()) < 0.9 * steps * sc["pos"].shape[0]
