@@ -154,3 +154,29 @@ def test_tile_culling_is_exact_and_queries_less():
     ea, eb = a.exact_queries(), b.exact_queries()
     print("exact queries exact/tile-culled", ea, eb)
     assert 0 < eb < ea, (ea, eb)
+
+
+def test_tile_culling_with_scenes_without_obstacles_and_shared_tiles():
+    """Culling per tile where scenes end inside a 32-slot tile (tiles with
+    particles of two obstacles are never culled) and some scenes have no
+    obstacle (shape -1): the bits of the exact maps, plain and from a graph."""
+    from fullc0ntact_gb300 import dem, sdf
+    scs, obs, shape = _small_obstacle_batch(num_scenes=6, n_min=1000, n_max=5000, seed=9)
+    shape = [s if k % 3 != 1 else -1 for k, s in enumerate(shape)]
+    maps = sdf.obstacle_maps(obs, 64)
+    net, _ = sdf.shape_net(maps)
+    r_max = 1.0 / 256.0
+    skin, _ = sdf.calibrate_skin(net, maps, r_max, seed=301)
+    lip, _ = sdf.calibrate_lipschitz(net, maps, pairs_per_map=200_000)
+    net.set_tile_culling(lip)
+    for graph in (False, True):
+        a, b = dem.Batch(scs), dem.Batch(scs)
+        a.set_obstacles(maps, shape)
+        b.set_obstacles(maps, shape, net=net, skin=skin)
+        a.update(30, graph=graph)
+        b.update(30, graph=graph)
+        dem.check("tile culling, mixed tiles")
+        for x, y in ((a.pos, b.pos), (a.vel, b.vel)):
+            np.testing.assert_array_equal(x.cpu().numpy().view(np.uint32),
+                                          y.cpu().numpy().view(np.uint32))
+        assert b.exact_queries() <= a.exact_queries()
