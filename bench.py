@@ -712,7 +712,7 @@ def cpu_baseline(sc: dict, steps: int) -> dict:
     dt1 = time.perf_counter() - t0
     return {"value": n * steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{steps} full updates of the {n}-sphere scene "
-                      f"(collide on {threads} threads, other stages on 1)",
+                      f"(every stage on {threads} threads)",
             "seconds": dt,
             "single_core": {"value": n * 2 / dt1, "unit": UNIT, "cores": 1,
                             "sample": f"the next 2 updates of the same scene on one thread",
@@ -780,7 +780,7 @@ def run_reference(args):
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"the first {steps} of the job's {args.steps} steps, each a "
                                    f"full update of the {n}-sphere scene from the packed "
-                                   f"state (collide on {threads} threads, other stages on 1); "
+                                   f"state (every stage on {threads} threads); "
                                    f"later steps of the job hold crowded cells and cost more"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }

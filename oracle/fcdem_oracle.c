@@ -415,15 +415,187 @@ void orc_collide_f64(const SimParams *P, double *newVel64,
   run_collide(J, nthreads);
 }
 
+/* ---------------------------------------------------------------------- */
+/* The same stages on nthreads host threads (the CPU baseline uses every
+ * core).  Each gives the single-threaded function's bits: integrate, hash
+ * and the reorder's gather are independent per particle; the radix sort
+ * keeps its stable order with per-thread digit counts taken over
+ * consecutive chunks; a cell's start and end are written by the one
+ * element where the sorted hash changes. */
+typedef struct {
+  int t, nt;
+  unsigned n;
+  void *ctx;
+  void (*fn)(void *ctx, int t, unsigned lo, unsigned hi);
+} par_job;
+
+static void *par_thread(void *arg) {
+  par_job *J = (par_job *)arg;
+  unsigned chunk = (J->n + (unsigned)J->nt - 1) / (unsigned)J->nt;
+  unsigned lo = (unsigned)J->t * chunk;
+  unsigned hi = lo + chunk < J->n ? lo + chunk : J->n;
+  if (lo < hi) J->fn(J->ctx, J->t, lo, hi);
+  return NULL;
+}
+
+/* fn(ctx, t, lo, hi) for thread t's chunk of [0, n); chunk t is the t-th
+ * of nt equal consecutive ranges */
+static void parallel_chunks(unsigned n, int nt, void *ctx,
+                            void (*fn)(void *ctx, int t, unsigned lo, unsigned hi)) {
+  pthread_t th[256];
+  par_job jobs[256];
+  for (int t = 0; t < nt; ++t) {
+    jobs[t].t = t;
+    jobs[t].nt = nt;
+    jobs[t].n = n;
+    jobs[t].ctx = ctx;
+    jobs[t].fn = fn;
+    th[t] = 0;
+    if (t > 0 && pthread_create(&th[t], NULL, par_thread, &jobs[t]) != 0) {
+      th[t] = 0;
+      par_thread(&jobs[t]);
+    }
+  }
+  par_thread(&jobs[0]);
+  for (int t = 1; t < nt; ++t)
+    if (th[t]) pthread_join(th[t], NULL);
+}
+
+typedef struct {
+  const SimParams *P;
+  float *pos, *vel, dt;
+  int radius_from_w;
+  unsigned *hash, *index;
+} stage_ctx;
+
+static void integrate_hash_chunk(void *c, int t, unsigned lo, unsigned hi) {
+  stage_ctx *S = (stage_ctx *)c;
+  (void)t;
+  orc_integrate(S->P, S->pos + 4 * (size_t)lo, S->vel + 4 * (size_t)lo, S->dt, hi - lo,
+                S->radius_from_w);
+  for (unsigned i = lo; i < hi; ++i) {
+    int g[3];
+    grid_pos(S->P, S->pos[4 * (size_t)i], S->pos[4 * (size_t)i + 1],
+             S->pos[4 * (size_t)i + 2], g);
+    S->hash[i] = grid_hash(S->P, g[0], g[1], g[2]);
+    S->index[i] = i;
+  }
+}
+
+typedef struct {
+  const unsigned *ka, *va;
+  unsigned *kb, *vb;
+  int shift;
+  size_t (*count)[256];  /* per thread: digit counts, then output offsets */
+} sort_ctx;
+
+static void sort_count_chunk(void *c, int t, unsigned lo, unsigned hi) {
+  sort_ctx *S = (sort_ctx *)c;
+  size_t *cnt = S->count[t];
+  memset(cnt, 0, 256 * sizeof(size_t));
+  for (unsigned i = lo; i < hi; ++i) cnt[(S->ka[i] >> S->shift) & 255u]++;
+}
+
+static void sort_scatter_chunk(void *c, int t, unsigned lo, unsigned hi) {
+  sort_ctx *S = (sort_ctx *)c;
+  size_t *off = S->count[t];
+  for (unsigned i = lo; i < hi; ++i) { /* ascending i within the chunk: stable */
+    size_t dst = off[(S->ka[i] >> S->shift) & 255u]++;
+    S->kb[dst] = S->ka[i];
+    S->vb[dst] = S->va[i];
+  }
+}
+
+static void sort_pairs_par(unsigned *keys, unsigned *vals, unsigned n, int nt) {
+  if (n < 2) return;
+  unsigned *k2 = (unsigned *)malloc(sizeof(unsigned) * (size_t)n);
+  unsigned *v2 = (unsigned *)malloc(sizeof(unsigned) * (size_t)n);
+  size_t (*count)[256] = (size_t(*)[256])malloc(sizeof(size_t) * 256 * (size_t)nt);
+  unsigned *ka = keys, *va = vals, *kb = k2, *vb = v2;
+  for (int shift = 0; shift < 32; shift += 8) {
+    sort_ctx S = {ka, va, kb, vb, shift, count};
+    parallel_chunks(n, nt, &S, sort_count_chunk);
+    size_t total[256];
+    memset(total, 0, sizeof(total));
+    for (int t = 0; t < nt; ++t)
+      for (int d = 0; d < 256; ++d) total[d] += count[t][d];
+    int trivial = 0;
+    for (int d = 0; d < 256; ++d)
+      if (total[d] == n) trivial = 1;
+    if (trivial) continue; /* one digit value: the pass is the identity */
+    /* digit-major, thread-minor offsets: the stable order of the
+     * single-threaded pass */
+    size_t run = 0;
+    for (int d = 0; d < 256; ++d)
+      for (int t = 0; t < nt; ++t) {
+        size_t c = count[t][d];
+        count[t][d] = run;
+        run += c;
+      }
+    parallel_chunks(n, nt, &S, sort_scatter_chunk);
+    unsigned *tmp = ka; ka = kb; kb = tmp;
+    tmp = va; va = vb; vb = tmp;
+  }
+  if (ka != keys) {
+    memcpy(keys, ka, sizeof(unsigned) * (size_t)n);
+    memcpy(vals, va, sizeof(unsigned) * (size_t)n);
+  }
+  free(count);
+  free(k2);
+  free(v2);
+}
+
+typedef struct {
+  unsigned *cellStart, *cellEnd;
+  float *sortedPos, *sortedVel;
+  const unsigned *hash, *index;
+  const float *oldPos, *oldVel;
+  unsigned n, numCells;
+} reorder_ctx;
+
+static void reorder_clear_chunk(void *c, int t, unsigned lo, unsigned hi) {
+  reorder_ctx *R = (reorder_ctx *)c;
+  (void)t;
+  memset(R->cellStart + lo, 0xff, sizeof(unsigned) * (size_t)(hi - lo));
+}
+
+static void reorder_chunk(void *c, int t, unsigned lo, unsigned hi) {
+  reorder_ctx *R = (reorder_ctx *)c;
+  (void)t;
+  for (unsigned i = lo; i < hi; ++i) {
+    unsigned h = R->hash[i];
+    if (i == 0 || h != R->hash[i - 1]) {
+      R->cellStart[h] = i;
+      if (i > 0) R->cellEnd[R->hash[i - 1]] = i;
+    }
+    if (i == R->n - 1) R->cellEnd[h] = i + 1;
+    unsigned s = R->index[i];
+    memcpy(R->sortedPos + 4 * (size_t)i, R->oldPos + 4 * (size_t)s, 16);
+    memcpy(R->sortedVel + 4 * (size_t)i, R->oldVel + 4 * (size_t)s, 16);
+  }
+}
+
 void orc_update(const SimParams *P, float dt, float *pos, float *vel,
                 float *sortedPos, float *sortedVel, unsigned *hash,
                 unsigned *index, unsigned *cellStart, unsigned *cellEnd,
                 unsigned n, int radius_from_w, int nthreads) {
-  orc_integrate(P, pos, vel, dt, n, radius_from_w);
-  orc_calc_hash(P, hash, index, pos, n);
-  orc_sort_pairs(hash, index, n);
-  orc_reorder(cellStart, cellEnd, sortedPos, sortedVel, hash, index, pos, vel,
-              n, P->numCells);
+  int nt = nthreads < 1 ? 1 : (nthreads > 256 ? 256 : nthreads);
+  if ((unsigned)nt > n / 4096u + 1u) nt = (int)(n / 4096u) + 1;  /* small n: fewer */
+  if (nt == 1) {
+    orc_integrate(P, pos, vel, dt, n, radius_from_w);
+    orc_calc_hash(P, hash, index, pos, n);
+    orc_sort_pairs(hash, index, n);
+    orc_reorder(cellStart, cellEnd, sortedPos, sortedVel, hash, index, pos, vel,
+                n, P->numCells);
+  } else {
+    stage_ctx S = {P, pos, vel, dt, radius_from_w, hash, index};
+    parallel_chunks(n, nt, &S, integrate_hash_chunk);
+    sort_pairs_par(hash, index, n, nt);
+    reorder_ctx R = {cellStart, cellEnd, sortedPos, sortedVel, hash, index,
+                     pos, vel, n, P->numCells};
+    parallel_chunks(P->numCells, nt, &R, reorder_clear_chunk);
+    parallel_chunks(n, nt, &R, reorder_chunk);
+  }
   orc_collide(P, vel, NULL, sortedPos, sortedVel, index, cellStart, cellEnd, n,
               radius_from_w, 1, nthreads);
 }

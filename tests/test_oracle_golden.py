@@ -101,3 +101,19 @@ def test_oracle_f64_twin_close_to_f32():
     scale = np.median(np.linalg.norm(f64, axis=1))
     err = np.linalg.norm(f32 - f64, axis=1) / np.maximum(np.linalg.norm(f64, axis=1), scale)
     assert err.max() < 1e-4
+
+
+def test_threaded_update_equals_single_thread():
+    """The oracle's full update on several host threads (integrate, hash,
+    the radix sort, the reorder and collide split into chunks) ends in the
+    bits of the single-threaded one, over a few steps of the packed scene."""
+    from fullc0ntact_gb300 import scenes
+    from fcdem_testutil import oracle_params
+    sc = scenes.packed_scene(60_000, grid=64)
+    P = oracle_params(bytes(sc["params"]))
+    a = (sc["pos"].copy(), sc["vel"].copy())
+    b = (sc["pos"].copy(), sc["vel"].copy())
+    O.update(P, a[0], a[1], sc["dt"], steps=3, radius_from_w=True, nthreads=1)
+    O.update(P, b[0], b[1], sc["dt"], steps=3, radius_from_w=True, nthreads=5)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
