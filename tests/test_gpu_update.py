@@ -219,3 +219,20 @@ def test_staged_rows_with_many_contacts_equal_staged_calls(crowd):
                 np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
     finally:
         dem.lib.fcdemSetCrowdPath(1)
+
+
+@pytest.mark.parametrize("n", [1, 2, 31, 33, 129, 1000])
+def test_fused_update_with_partial_warps(n):
+    """Particle counts that leave the last warp, or the only one, partly
+    empty (the collide's lane mask, its row copies and the crowded lists
+    then cover fewer than 32 lanes): five fused updates against the staged
+    calls, in a box small enough that the particles touch."""
+    from fullc0ntact_gb300 import dem, scenes
+    sc = scenes.random_box(n, grid=(8, 8, 8), radius=0.1, cell=0.25, seed=n, poly=(n % 2 == 1))
+    a, b = dem.DeviceScene(sc), dem.DeviceScene(sc)
+    for _ in range(5):
+        a.stages()
+    b.update(5)
+    dem.check("partial warps")
+    for x, y in zip(_state(a), _state(b)):
+        np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
