@@ -150,19 +150,28 @@ kAddTileBlocks(unsigned *__restrict__ tileOff, unsigned tiles,
 }
 
 // off[c] = tileOff[tile] + exclusive prefix of cnt within the tile, cnt
-// cleared.  A tile without particles only writes its constant offsets.
+// cleared.  A tile without particles only writes its constant offsets, and
+// not even those when off already holds them: tileOffPrev[tile] records the
+// constant a tile's offsets were last written with (0xffffffff after a tile
+// with particles, whose offsets vary), so a tile that stays empty with the
+// same prefix -- the common case in sparse grids: the cells above and below
+// a pile -- is left as it is.
 // Round q of a tile covers cells q*1024 .. +1024, thread t the four at 4t
 // (16-byte accesses, coalesced).
 __global__ void __launch_bounds__(kScanThreads)
 kScanCells(unsigned *__restrict__ cnt, unsigned *__restrict__ off, unsigned m,
-           const unsigned *__restrict__ tileOff) {
+           const unsigned *__restrict__ tileOff, unsigned *__restrict__ tileOffPrev) {
   __shared__ unsigned sWarp[kScanThreads / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const unsigned tile = blockIdx.x;
   constexpr int kRounds = kScanItems / 4;
   const size_t tbase = (size_t)tile * kScanTile;
   const unsigned t0 = __ldg(tileOff + tile), t1 = __ldg(tileOff + tile + 1);
+  const unsigned prev = tileOffPrev[tile];  // read by every thread before thread 0 writes
   if (t0 == t1) {  // empty tile: every cell starts (and ends) at t0
+    if (prev == t0) return;  // off already holds t0 in every cell of the tile
+    __syncthreads();
+    if (tid == 0) tileOffPrev[tile] = t0;
 #pragma unroll
     for (int q = 0; q < kRounds; ++q) {
       const size_t c0 = tbase + (size_t)q * (kScanThreads * 4) + (size_t)tid * 4;
@@ -175,6 +184,8 @@ kScanCells(unsigned *__restrict__ cnt, unsigned *__restrict__ off, unsigned m,
     }
     return;
   }
+  __syncthreads();
+  if (tid == 0 && prev != 0xffffffffu) tileOffPrev[tile] = 0xffffffffu;  // offsets vary
   uint4 v[kRounds];
   unsigned excl[kRounds];
 #pragma unroll
@@ -650,7 +661,7 @@ bool countBuffersIn(void *&buf, size_t &bytes, unsigned &cells, unsigned n, unsi
   auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
   const unsigned largeCap = largeCapacity(n);
   const unsigned tileBlocks = (tiles + kTileBlock - 1) / kTileBlock;
-  const size_t need = 2 * al(m * 4) + 4 * al((size_t)n * 4) + 2 * al((size_t)(tiles + 1) * 4) +
+  const size_t need = 2 * al(m * 4) + 4 * al((size_t)n * 4) + 3 * al((size_t)(tiles + 1) * 4) +
                       al(((size_t)largeCap + 1) * 4) + al((size_t)tileBlocks * 4) +
                       al((size_t)kBitmapSlots * 2 * bitmapWords(n) * 4);
   if (buf == nullptr || bytes < need || cells != numCells) {
@@ -667,6 +678,9 @@ bool countBuffersIn(void *&buf, size_t &bytes, unsigned &cells, unsigned n, unsi
     bytes = need;
     cells = numCells;
     if (!cudaOk(cudaMemset(buf, 0, need))) return false;  // cnt starts at zero
+    // no tile's offsets are known yet (see kScanCells)
+    const size_t prevAt = 2 * al(m * 4) + 2 * al((size_t)(tiles + 1) * 4);
+    if (!cudaOk(cudaMemset((char *)buf + prevAt, 0xff, (size_t)(tiles + 1) * 4))) return false;
   }
   // The arrays that must stay zero between calls (cnt, tileCnt) sit first,
   // at offsets that depend on the cell count only, so that a call with
@@ -679,6 +693,8 @@ bool countBuffersIn(void *&buf, size_t &bytes, unsigned &cells, unsigned n, unsi
   b.off = (unsigned *)p;
   p += al(m * 4);
   b.tileOff = (unsigned *)p;
+  p += al((size_t)(tiles + 1) * 4);
+  b.tileOffPrev = (unsigned *)p;
   p += al((size_t)(tiles + 1) * 4);
   b.rank = (unsigned *)p;
   p += al((size_t)n * 4);
@@ -742,7 +758,8 @@ bool countPipelineSort(Context &c, const CountBuffers &b, const unsigned *origOf
     kAddTileBlocks<<<blocks, kTileBlock, 0, st>>>(b.tileOff, b.scanTiles, b.tileBlockSum);
     if (!launchOk()) return false;
   }
-  kScanCells<<<b.scanTiles, kScanThreads, 0, st>>>(b.cnt, b.off, m, b.tileOff);
+  kScanCells<<<b.scanTiles, kScanThreads, 0, st>>>(b.cnt, b.off, m, b.tileOff,
+                                                    b.tileOffPrev);
   if (!launchOk()) return false;
   // hash holds the new hashes in entry order until the fix-up overwrites it
   kScatterCells<<<(n + 255) / 256, 256, 0, st>>>(hash, b.rank, origOf, b.off, b.slotKey,

@@ -181,6 +181,7 @@ void launchCollideBatch(int mode, bool radiusFromW, const BatchScene *scenes,
 struct CountBuffers {
   unsigned *cnt, *off, *rank, *slotKey, *slotIdx, *slotPrev;
   unsigned *tileCnt, *tileOff;  // per 4096-cell tile: counts and their prefix
+  unsigned *tileOffPrev;        // per tile: the constant its offsets hold, or 0xffffffff
   unsigned *large;              // [0] = count, [1..largeCap] = cells too full for the re-rank
   unsigned *tileBlockSum;       // per 1024 tiles: their total (many-tile scans)
   unsigned *bitmaps;            // kFixupLarge: per-CTA bitmap + word prefix of particle indices
