@@ -244,12 +244,14 @@ def measure_batched(num_scenes: int, steps: int, plain_steps: int, dev: int) -> 
     vel0 = torch.from_numpy(np.concatenate([s["vel"] for s in sl]))
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
-    def timed(fn):
+    def timed(fn, name="fcdem_batch"):
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push(name)  # profilers can select the range
         e0.record()
         fn()
         e1.record()
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         return e0.elapsed_time(e1)
 
     batch = dem.Batch(sl, f"cuda:{dev}")
@@ -257,12 +259,12 @@ def measure_batched(num_scenes: int, steps: int, plain_steps: int, dev: int) -> 
     batch.update(steps, graph=True)  # records the job's graph
     batch.pos.copy_(pos0)
     batch.vel.copy_(vel0)
-    job_ms = timed(lambda: batch.update(steps, graph=True))
+    job_ms = timed(lambda: batch.update(steps, graph=True), "fcdem_batch_job")
     dem.check("batched job")
     batch.update(plain_steps, graph=True)  # records the comparison graph
     batch.pos.copy_(pos0)
     batch.vel.copy_(vel0)
-    batched_ms = timed(lambda: batch.update(plain_steps, graph=True))
+    batched_ms = timed(lambda: batch.update(plain_steps, graph=True), "fcdem_batch_first")
     dem.check("batched")
     del batch
     singles = [dem.Batch([sc], f"cuda:{dev}") for sc in sl]
@@ -626,10 +628,14 @@ def measure_batched_obstacles(num_scenes: int, steps: int, dev: int) -> dict:
         b.vel.copy_(vel0)
         b.exact_queries(reset=True)
         torch.cuda.synchronize()
+        # profilers can select each run's range
+        name = "fcdem_obstacles_" + ("exact" if not use_net else "tiles" if tiles else "net")
+        torch.cuda.nvtx.range_push(name)
         e0.record()
         b.update(steps, graph=True)
         e1.record()
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         dem.check("obstacle batch")
         return b, e0.elapsed_time(e1), b.exact_queries()
 
