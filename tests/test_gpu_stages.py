@@ -148,3 +148,28 @@ def test_errors_are_reported_not_fatal():
     dem.lib.registerGLBufferObject(1, None)
     assert dem.lib.fcdemGetLastError() == 4
     assert dem.lib.fcdemGetLastError() == 0
+
+
+def test_tuning_and_culling_arguments_are_checked():
+    """The tuning and culling entry points reject bad arguments with an error
+    code and change nothing: a collide autotune of no particles, an unknown
+    collide configuration, a negative Lipschitz bound or no network."""
+    import ctypes as C
+    from fullc0ntact_gb300 import dem
+    lib = dem.lib
+    lib.fcdemGetLastError()  # clear anything pending
+    null = C.c_void_p()
+    assert lib.fcdemAutotuneCollide(*([null] * 8), 0.5, 0, 8, None) == -1
+    assert lib.fcdemGetLastError() == 1  # FCDEM_ERR_INVALID_VALUE
+    lim = C.c_uint(7)
+    assert lib.fcdemGetCollideConfig(30, C.byref(lim), None, None) == -1
+    assert lim.value == 7 and lib.fcdemGetLastError() == 1
+    assert lib.fcdemSetCollideConfig(-5) == 30  # out of range: the default
+    lib.fcdemSdfSetTileCulling(None, 1.0)
+    assert lib.fcdemGetLastError() == 1
+    from fullc0ntact_gb300 import sdf
+    net = sdf.SdfNet(3, 64, 2, seed=1)
+    lib.fcdemSdfSetTileCulling(net.handle, -1.0)
+    assert lib.fcdemGetLastError() == 1
+    net.set_tile_culling(0.0)
+    assert lib.fcdemGetLastError() == 0
