@@ -155,7 +155,7 @@ def test_tuning_and_culling_arguments_are_checked():
     code and change nothing: a collide autotune of no particles, an unknown
     collide configuration, a negative Lipschitz bound or no network."""
     import ctypes as C
-    from fullc0ntact_gb300 import dem
+    from fullc0ntact_gb300 import dem, sdf  # sdf sets the culling calls' argument types
     lib = dem.lib
     lib.fcdemGetLastError()  # clear anything pending
     null = C.c_void_p()
@@ -167,7 +167,6 @@ def test_tuning_and_culling_arguments_are_checked():
     assert lib.fcdemSetCollideConfig(-5) == 30  # out of range: the default
     lib.fcdemSdfSetTileCulling(None, 1.0)
     assert lib.fcdemGetLastError() == 1
-    from fullc0ntact_gb300 import sdf
     net = sdf.SdfNet(3, 64, 2, seed=1)
     lib.fcdemSdfSetTileCulling(net.handle, -1.0)
     assert lib.fcdemGetLastError() == 1
